@@ -1,0 +1,168 @@
+// Team FFT: an N-point complex FFT computed by a team of T lanes of one warp
+// in shared memory (Stockham auto-sort, radix-16 passes then one radix-8/4/2
+// pass, natural order in and out, unnormalised; the conventions of the
+// forward/inverse transforms the reference takes from cuFFT,
+// fft_interpolate_routines.cu:89-105 and do_freq_xcorr.cu:99-113).
+//
+// Pass p with stride Ns and radix R: lane j (j < N/R, several per lane when
+// N/R > T) loads x[j + r N/R] for r < R, multiplies by w_{Ns R}^{(j mod Ns) r},
+// does an R-point DFT in registers and stores it to y[(j - j mod Ns) R + j mod Ns + r Ns].
+// Shared-memory index i is padded to i + i/16, which makes every pass of
+// N = 128..1024 conflict-free for 8-byte accesses.
+// Pass twiddles live in a table laid out [pass][r-1][k] so that lanes with
+// consecutive k read consecutive words; the host builds it in double.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace xcg {
+
+__host__ __device__ constexpr int fft_pad(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int fft_padded_len(int n) { return n + (n >> 4); }
+
+// radix list: 16 while the remainder is >= 16, then the remainder
+__host__ __device__ constexpr int fft_npasses(int n) {
+    int p = 0;
+    while (n >= 16) { n >>= 4; p++; }
+    return p + (n > 1 ? 1 : 0);
+}
+__host__ __device__ constexpr int fft_radix(int n, int pass) {
+    for (int p = 0; p < pass; p++) n = (n >= 16) ? (n >> 4) : 1;
+    return n >= 16 ? 16 : n;
+}
+// number of twiddle entries of all passes (first pass needs none)
+__host__ __device__ constexpr int fft_twiddle_len(int n) {
+    int len = 0, ns = 1;
+    for (int p = 0; p < fft_npasses(n); p++) {
+        int r = fft_radix(n, p);
+        if (p > 0) len += (r - 1) * ns;
+        ns *= r;
+    }
+    return len;
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmulf_conj(float2 a, float2 b) {   // a * conj(b)
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+
+// cos / sin of 2*pi*m/16
+__device__ constexpr float kC1 = 0.923879532511286756128f;   // cos(pi/8)
+__device__ constexpr float kS1 = 0.382683432365089771728f;   // sin(pi/8)
+__device__ constexpr float kR2 = 0.707106781186547524401f;   // sqrt(2)/2
+
+// b * exp(DIR * 2*pi*i * M16 / 16), with the trivial rotations written out
+template <int M16, int DIR>
+__device__ __forceinline__ float2 rot16(float2 b) {
+    constexpr int m = ((M16 % 16) + 16) % 16;
+    if constexpr (m == 0) {
+        return b;
+    } else if constexpr (m == 8) {
+        return make_float2(-b.x, -b.y);
+    } else if constexpr (m == 4) {      // exp(DIR i pi/2) = DIR * i
+        return DIR < 0 ? make_float2(b.y, -b.x) : make_float2(-b.y, b.x);
+    } else if constexpr (m == 12) {     // exp(DIR i 3pi/2) = -DIR * i
+        return DIR < 0 ? make_float2(-b.y, b.x) : make_float2(b.y, -b.x);
+    } else {
+        constexpr int q = m & 3;        // angle within a quadrant: q * pi/8
+        constexpr float cq = (q == 1) ? kC1 : (q == 2) ? kR2 : kS1;
+        constexpr float sq = (q == 1) ? kS1 : (q == 2) ? kR2 : kC1;
+        // rotate into quadrant m/4
+        constexpr int quad = m >> 2;
+        constexpr float c = (quad == 0) ? cq : (quad == 1) ? -sq : (quad == 2) ? -cq : sq;
+        constexpr float s0 = (quad == 0) ? sq : (quad == 1) ? cq : (quad == 2) ? -sq : -cq;
+        constexpr float s = DIR * s0;
+        return make_float2(b.x * c - b.y * s, b.x * s + b.y * c);
+    }
+}
+
+template <int R>
+__host__ __device__ constexpr int bitrev_c(int i) {
+    int r = 0;
+    for (int b = 1, k = R >> 1; b < R; b <<= 1, k >>= 1)
+        if (i & b) r |= k;
+    return r;
+}
+
+// One butterfly stage of length LEN inside an R-point register DFT.
+template <int R, int LEN, int DIR, int K>
+struct DftStage {
+    static __device__ __forceinline__ void run(float2 *t, int i) {
+        if constexpr (K < LEN / 2) {
+            float2 a = t[i + K];
+            float2 b = rot16<K * (16 / LEN), DIR>(t[i + K + LEN / 2]);
+            t[i + K] = make_float2(a.x + b.x, a.y + b.y);
+            t[i + K + LEN / 2] = make_float2(a.x - b.x, a.y - b.y);
+            DftStage<R, LEN, DIR, K + 1>::run(t, i);
+        }
+    }
+};
+
+template <int R, int LEN, int DIR>
+__device__ __forceinline__ void dft_level(float2 *t) {
+    if constexpr (LEN <= R) {
+#pragma unroll
+        for (int i = 0; i < R; i += LEN) DftStage<R, LEN, DIR, 0>::run(t, i);
+        dft_level<R, LEN * 2, DIR>(t);
+    }
+}
+
+// R-point DFT of v (R = 2, 4, 8, 16) in registers, natural order in and out.
+template <int R, int DIR>
+__device__ __forceinline__ void dft_reg(float2 *v) {
+    float2 t[R];
+#pragma unroll
+    for (int i = 0; i < R; i++) t[i] = v[bitrev_c<R>(i)];
+    dft_level<R, 2, DIR>(t);
+#pragma unroll
+    for (int i = 0; i < R; i++) v[i] = t[i];
+}
+
+// One Stockham pass.  tw: this pass's twiddles [R-1][Ns] (forward sign).
+template <int N, int R, int DIR>
+__device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                              int Ns, const float2 *__restrict__ tw, int lane, int T) {
+    constexpr int NR = N / R;
+    for (int j = lane; j < NR; j += T) {
+        float2 v[R];
+        const int k = j & (Ns - 1);
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = src[fft_pad(j + r * NR)];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                float2 w = tw[(r - 1) * Ns + k];
+                v[r] = DIR < 0 ? cmulf(v[r], w) : cmulf_conj(v[r], w);
+            }
+        }
+        dft_reg<R, DIR>(v);
+        const int idxD = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) dst[fft_pad(idxD + r * Ns)] = v[r];
+    }
+}
+
+template <int N, int DIR, int PASS>
+__device__ __forceinline__ float2 *team_fft_from(float2 *a, float2 *b, const float2 *tw, int Ns, int lane, int T) {
+    if constexpr (PASS >= fft_npasses(N)) {
+        return a;
+    } else {
+        constexpr int R = fft_radix(N, PASS);
+        stockham_pass<N, R, DIR>(a, b, Ns, tw, lane, T);
+        __syncwarp();
+        const float2 *tw_next = (PASS == 0) ? tw : tw + (R - 1) * Ns;
+        return team_fft_from<N, DIR, PASS + 1>(b, a, tw_next, Ns * R, lane, T);
+    }
+}
+
+// N-point FFT of the padded sequence in a (scratch b, same size); returns the
+// buffer holding the result.  tw: the size-N table (fft_twiddle_len(N) entries).
+// Every lane of the warp must call it (it ends each pass with __syncwarp).
+template <int N, int DIR>
+__device__ __forceinline__ float2 *team_fft(float2 *a, float2 *b, const float2 *tw, int lane, int T) {
+    return team_fft_from<N, DIR, 0>(a, b, tw, 1, lane, T);
+}
+
+}  // namespace xcg

@@ -1,0 +1,421 @@
+// C ABI of the GB300 xcorr library (include/xcorr_gb300.h): context,
+// transform tables, scratch, batching and launches.
+//
+// The context replaces the reference's device plan and allocations
+// (d_allocate_arrays xcorr.cu:65-119, estimate_istep :161-230) and its strip
+// loop (do_correlation :299-378).  Windows run in batches sized to the
+// scratch; each batch is four kernel launches on one stream.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "team_fft.cuh"
+#include "xcorr_gb300.h"
+#include "xcorr_kernels.cuh"
+
+using cd = std::complex<double>;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+xcg_status cuda_fail(cudaError_t e, const char *what) {
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+    g_last_error = buf;
+    return (e == cudaErrorMemoryAllocation) ? XCG_ERR_NOMEM : XCG_ERR_CUDA;
+}
+
+#define XCG_CK(call, what)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what);   \
+    } while (0)
+
+bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+int ilog2(int v) { int l = 0; while ((1 << l) < v) l++; return l; }
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Stockham pass twiddles of an n-point FFT, [pass >= 1][r-1][k], forward sign.
+std::vector<float2> stockham_twiddles(int n) {
+    std::vector<float2> t;
+    int ns = 1;
+    for (int p = 0; p < xcg::fft_npasses(n); p++) {
+        const int r = xcg::fft_radix(n, p);
+        if (p > 0)
+            for (int rr = 1; rr < r; rr++)
+                for (int k = 0; k < ns; k++) {
+                    const double a = -2.0 * M_PI * (double)k * rr / ((double)ns * r);
+                    t.push_back(make_float2((float)cos(a), (float)sin(a)));
+                }
+        ns *= r;
+    }
+    return t;
+}
+
+// Operator of d_fft_interpolate_1d_strip (fft_interpolate_routines.cu:76-113)
+// from n samples to m = ifc*n: FFT, bins [0,n/2) kept, bins [n/2,n) moved to
+// the top (frequency f-n), inverse FFT of m, scale 1/n.  op[X][c].
+std::vector<float2> interp_operator(int n, int m) {
+    std::vector<float2> op((size_t)m * n);
+    for (int X = 0; X < m; X++)
+        for (int c = 0; c < n; c++) {
+            cd s = 0;
+            for (int f = 0; f < n; f++) {
+                const int fp = (f < n / 2) ? f : f - n;
+                s += std::polar(1.0, -2.0 * M_PI * f * c / n) * std::polar(1.0, 2.0 * M_PI * fp * X / m);
+            }
+            s /= (double)n;
+            op[(size_t)X * n + c] = make_float2((float)s.real(), (float)s.imag());
+        }
+    return op;
+}
+
+// DFT of the 0/1 mask along one axis (make_mask, xcorr.cu:385-401): ones on [lo, n-lo).
+std::vector<float2> box_spectrum(int n, int lo) {
+    std::vector<float2> b(n);
+    for (int k = 0; k < n; k++) {
+        cd s = 0;
+        for (int c = lo; c < n - lo; c++) s += std::polar(1.0, -2.0 * M_PI * (double)k * c / n);
+        b[k] = make_float2((float)s.real(), (float)s.imag());
+    }
+    return b;
+}
+
+}  // namespace
+
+struct xcg_ctx {
+    xcg_params prm;
+    int device;
+    xcg::Plan base;           // sizes and tables; per-batch fields filled at launch
+    // tables
+    float2 *d_tables = nullptr;
+    // scratch
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    int max_batch = 0;
+    size_t off_zrow, off_amp1, off_amp2c, off_part, off_oob, off_means, off_qspec, off_surf, off_md, off_mdnext, off_corr0n;
+    // host-entry buffers
+    void *d_img[2] = {nullptr, nullptr};
+    size_t img_bytes[2] = {0, 0};
+    xcg_loc *d_locs = nullptr;
+    xcg_result *d_res = nullptr;
+    int io_cap = 0;
+    cudaStream_t stream = nullptr;
+    // profiling
+    int profiling = 0;
+    std::vector<cudaEvent_t> events;
+    xcg_stats stats;
+};
+
+extern "C" {
+
+const char *xcg_status_string(xcg_status s) {
+    switch (s) {
+        case XCG_OK: return "ok";
+        case XCG_ERR_ARG: return "invalid argument";
+        case XCG_ERR_UNSUPPORTED: return "unsupported parameter combination";
+        case XCG_ERR_CUDA: return "CUDA error";
+        case XCG_ERR_NOMEM: return "out of memory";
+        case XCG_ERR_NO_DEVICE: return "no usable CUDA device";
+        case XCG_ERR_TOO_LARGE: return "size exceeds a fixed limit";
+    }
+    return "unknown status";
+}
+
+const char *xcg_last_error(void) { return g_last_error.c_str(); }
+
+void xcg_default_params(xcg_params *p) {
+    if (!p) return;
+    p->xsearch = 64; p->ysearch = 64;
+    p->nx_corr = 128; p->ny_corr = 128;
+    p->ri = 2;
+    p->interp_flag = 1;
+    p->interp_factor = 16;
+    p->n2x = 8; p->n2y = 8;
+    p->format = 0;
+}
+
+static size_t per_window_bytes(const xcg::Plan &B) {
+    size_t s = 0;
+    s += align256((size_t)B.npy * B.npx * sizeof(float2));
+    s += align256((size_t)B.npy * B.npx * sizeof(float));
+    s += align256((size_t)B.ny_corr * B.nx_corr * sizeof(float));
+    s += align256((size_t)2 * B.nchunks * sizeof(float));
+    s += align256((size_t)B.nchunks);
+    s += align256(2 * sizeof(double));
+    s += align256((size_t)B.nyc * B.qpitch * sizeof(float2));
+    s += align256((size_t)B.nyc * B.nxc * sizeof(float));
+    s += align256(64 * sizeof(float)) + align256(64) + align256(sizeof(double));
+    return s;
+}
+
+xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xcg_ctx **out) {
+    if (!p || !out) return XCG_ERR_ARG;
+    *out = nullptr;
+    const int xs = p->xsearch, ys = p->ysearch;
+    if (!pow2(xs) || !pow2(ys) || xs < 32 || ys < 32 || xs > 256 || ys > 256) {
+        g_last_error = "xsearch/ysearch must be powers of two in 32..256";
+        return XCG_ERR_ARG;
+    }
+    if (p->nx_corr != 2 * xs || p->ny_corr != 2 * ys) {
+        g_last_error = "nx_corr/ny_corr must be 2*xsearch/2*ysearch (parse_xcorr_input.c:143,153)";
+        return XCG_ERR_UNSUPPORTED;
+    }
+    if (!(p->ri == 1 || p->ri == 2 || p->ri == 4 || p->ri == 8)) { g_last_error = "ri must be 1, 2, 4 or 8"; return XCG_ERR_ARG; }
+    if (p->interp_flag && !(p->interp_factor == 8 || p->interp_factor == 16 || p->interp_factor == 32 || p->interp_factor == 64)) {
+        g_last_error = "interp_factor must be 8, 16, 32 or 64";
+        return XCG_ERR_ARG;
+    }
+    if (p->n2x != 8 || p->n2y != 8) { g_last_error = "n2x = n2y = 8 only"; return XCG_ERR_UNSUPPORTED; }
+    if (p->format != 0 && p->format != 1) { g_last_error = "format must be 0 or 1"; return XCG_ERR_ARG; }
+
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev <= device || device < 0) {
+        g_last_error = (e != cudaSuccess) ? cudaGetErrorString(e) : "device index out of range";
+        return XCG_ERR_NO_DEVICE;
+    }
+    XCG_CK(cudaSetDevice(device), "cudaSetDevice");
+
+    xcg_ctx *c = new xcg_ctx();
+    c->prm = *p;
+    c->device = device;
+    memset(&c->stats, 0, sizeof c->stats);
+    xcg::Plan &B = c->base;
+    memset(&B, 0, sizeof B);
+    B.xsearch = xs; B.ysearch = ys;
+    B.npx = 4 * xs; B.npy = 4 * ys;
+    B.nxc = 2 * xs; B.nyc = 2 * ys;
+    B.nx_corr = 2 * xs; B.ny_corr = 2 * ys;
+    B.ri = p->ri; B.log2ri = ilog2(p->ri);
+    B.interp_flag = p->interp_flag;
+    B.ifc = p->interp_flag ? p->interp_factor : 16;
+    B.n2x = p->n2x; B.n2y = p->n2y;
+    B.nx2 = B.n2x * B.ifc; B.ny2 = B.n2y * B.ifc;
+    B.format = p->format;
+    B.nchunks = B.npx * B.npy / 1024;
+    B.qpitch = B.npx / 2 + 16;
+
+    // tables
+    std::vector<float2> tw_row = stockham_twiddles(B.npx), tw_col = stockham_twiddles(B.npy);
+    std::vector<float2> phase((size_t)(B.ri > 1 ? B.ri - 1 : 1) * B.npx);
+    for (int q = 1; q < B.ri; q++)
+        for (int f = 0; f < B.npx; f++) {
+            const int fp = (f < B.npx / 2) ? f : f - B.npx;
+            const cd v = std::polar(1.0 / B.npx, 2.0 * M_PI * fp * q / ((double)B.ri * B.npx));
+            phase[(size_t)(q - 1) * B.npx + f] = make_float2((float)v.real(), (float)v.imag());
+        }
+    std::vector<float2> bx = box_spectrum(B.npx, xs), by = box_spectrum(B.npy, ys);
+    std::vector<float2> kxo = interp_operator(B.n2x, B.nx2), kyo = interp_operator(B.n2y, B.ny2);
+    std::vector<float2> all;
+    size_t o_twr = all.size(); all.insert(all.end(), tw_row.begin(), tw_row.end()); all.resize(align256(all.size() * 8) / 8);
+    size_t o_twc = all.size(); all.insert(all.end(), tw_col.begin(), tw_col.end()); all.resize(align256(all.size() * 8) / 8);
+    size_t o_ph = all.size(); all.insert(all.end(), phase.begin(), phase.end()); all.resize(align256(all.size() * 8) / 8);
+    size_t o_bx = all.size(); all.insert(all.end(), bx.begin(), bx.end()); all.resize(align256(all.size() * 8) / 8);
+    size_t o_by = all.size(); all.insert(all.end(), by.begin(), by.end()); all.resize(align256(all.size() * 8) / 8);
+    size_t o_kx = all.size(); all.insert(all.end(), kxo.begin(), kxo.end()); all.resize(align256(all.size() * 8) / 8);
+    size_t o_ky = all.size(); all.insert(all.end(), kyo.begin(), kyo.end()); all.resize(align256(all.size() * 8) / 8);
+    xcg_status st = XCG_OK;
+#define XCG_CK_C(call, what)                                              \
+    do {                                                                  \
+        cudaError_t e_ = (call);                                          \
+        if (e_ != cudaSuccess) { st = cuda_fail(e_, what); goto fail; }   \
+    } while (0)
+    {
+        XCG_CK_C(cudaMalloc(&c->d_tables, all.size() * sizeof(float2)), "cudaMalloc tables");
+        XCG_CK_C(cudaMemcpy(c->d_tables, all.data(), all.size() * sizeof(float2), cudaMemcpyHostToDevice), "upload tables");
+        B.tw_row = c->d_tables + o_twr;
+        B.tw_col = c->d_tables + o_twc;
+        B.phase = c->d_tables + o_ph;
+        B.box_x = c->d_tables + o_bx;
+        B.box_y = c->d_tables + o_by;
+        B.kx = c->d_tables + o_kx;
+        B.ky = c->d_tables + o_ky;
+        XCG_CK_C(xcg::kernels_setup(B), "kernel attributes");
+
+        // scratch: up to max_batch windows, at most 8 GiB or 40% of free memory
+        const size_t pw = per_window_bytes(B);
+        size_t freeb = 0, totb = 0;
+        XCG_CK_C(cudaMemGetInfo(&freeb, &totb), "cudaMemGetInfo");
+        size_t budget = (size_t)8 << 30;
+        if (budget > freeb * 2 / 5) budget = freeb * 2 / 5;
+        int mb = max_batch > 0 ? max_batch : 4096;
+        if ((size_t)mb * pw > budget) mb = (int)(budget / pw);
+        if (mb < 1) { st = XCG_ERR_NOMEM; g_last_error = "not enough device memory for one window"; goto fail; }
+        c->max_batch = mb;
+        size_t off = 0;
+        auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes * (size_t)mb); return o; };
+        c->off_zrow = take((size_t)B.npy * B.npx * sizeof(float2));
+        c->off_amp1 = take((size_t)B.npy * B.npx * sizeof(float));
+        c->off_amp2c = take((size_t)B.ny_corr * B.nx_corr * sizeof(float));
+        c->off_part = take((size_t)2 * B.nchunks * sizeof(float));
+        c->off_oob = take((size_t)B.nchunks);
+        c->off_means = take(2 * sizeof(double));
+        c->off_qspec = take((size_t)B.nyc * B.qpitch * sizeof(float2));
+        c->off_surf = take((size_t)B.nyc * B.nxc * sizeof(float));
+        c->off_md = take(64 * sizeof(float));
+        c->off_mdnext = take(64);
+        c->off_corr0n = take(sizeof(double));
+        c->scratch_bytes = off;
+        XCG_CK_C(cudaMalloc(&c->d_scratch, off), "cudaMalloc scratch");
+        XCG_CK_C(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    }
+#undef XCG_CK_C
+    c->stats.scratch_bytes = c->scratch_bytes;
+    *out = c;
+    return XCG_OK;
+fail:
+    xcg_destroy(c);
+    return st;
+}
+
+void xcg_destroy(xcg_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_tables);
+    cudaFree(c->d_scratch);
+    cudaFree(c->d_img[0]);
+    cudaFree(c->d_img[1]);
+    cudaFree(c->d_locs);
+    cudaFree(c->d_res);
+    for (cudaEvent_t ev : c->events) cudaEventDestroy(ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+void xcg_set_profiling(xcg_ctx *c, int32_t enable) {
+    if (c) c->profiling = enable ? 1 : 0;
+}
+
+void xcg_get_stats(const xcg_ctx *c, xcg_stats *out) {
+    if (c && out) *out = c->stats;
+}
+
+xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, int32_t m_ny,
+                                const void *d_slave, int32_t s_nx, int32_t s_ny,
+                                int32_t x_offset, int32_t y_offset, double astretcha,
+                                const xcg_loc *d_locs, int32_t nlocs, int32_t strip_len,
+                                xcg_result *d_results, void *stream) {
+    if (!c || nlocs < 0 || (nlocs > 0 && (!d_master || !d_slave || !d_locs || !d_results))) return XCG_ERR_ARG;
+    if (m_nx <= 0 || m_ny <= 0 || s_nx <= 0 || s_ny <= 0 || strip_len < 0) return XCG_ERR_ARG;
+    XCG_CK(cudaSetDevice(c->device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    memset(&c->stats, 0, sizeof c->stats);
+    c->stats.scratch_bytes = c->scratch_bytes;
+    if (nlocs == 0) return XCG_OK;
+
+    int bw = c->max_batch;
+    if (strip_len > 0 && strip_len <= bw) bw = (bw / strip_len) * strip_len;   // keep strips inside a batch
+    xcg::Plan P = c->base;
+    P.master = d_master; P.m_nx = m_nx; P.m_ny = m_ny;
+    P.slave = d_slave; P.s_nx = s_nx; P.s_ny = s_ny;
+    P.x_offset = x_offset; P.y_offset = y_offset; P.astretcha = astretcha;
+    P.strip_len = strip_len;
+    P.nlocs_total = nlocs;
+    char *sc = (char *)c->d_scratch;
+    P.zrow = (float2 *)(sc + c->off_zrow);
+    P.amp1 = (float *)(sc + c->off_amp1);
+    P.amp2c = (float *)(sc + c->off_amp2c);
+    P.part = (float *)(sc + c->off_part);
+    P.oobmap = (unsigned char *)(sc + c->off_oob);
+    P.means = (double *)(sc + c->off_means);
+    P.qspec = (float2 *)(sc + c->off_qspec);
+    P.surf = (float *)(sc + c->off_surf);
+    P.md = (float *)(sc + c->off_md);
+    P.mdnext = (unsigned char *)(sc + c->off_mdnext);
+    P.corr0n = (double *)(sc + c->off_corr0n);
+
+    const int nb = (nlocs + bw - 1) / bw;
+    const int nk = P.interp_flag ? 4 : 3;
+    if (c->profiling) {
+        const size_t need = (size_t)nb * nk * 2;
+        while (c->events.size() < need) {
+            cudaEvent_t ev;
+            XCG_CK(cudaEventCreate(&ev), "cudaEventCreate");
+            c->events.push_back(ev);
+        }
+    }
+    int ei = 0;
+    for (int b = 0; b < nb; b++) {
+        P.win0 = b * bw;
+        P.nwin = (nlocs - P.win0 < bw) ? nlocs - P.win0 : bw;
+        P.locs = d_locs + P.win0;
+        P.out = d_results + P.win0;
+        for (int k = 0; k < nk; k++) {
+            if (c->profiling) cudaEventRecord(c->events[ei++], s);
+            switch (k) {
+                case 0: xcg::launch_rows(P, s); break;
+                case 1: xcg::launch_cols(P, s); break;
+                case 2: xcg::launch_peak(P, s); break;
+                case 3: xcg::launch_subpix(P, s); break;
+            }
+            if (c->profiling) cudaEventRecord(c->events[ei++], s);
+            c->stats.launches++;
+        }
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    c->stats.batches = nb;
+    c->stats.batch_windows = bw;
+    if (c->profiling) {
+        XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        ei = 0;
+        for (int b = 0; b < nb; b++)
+            for (int k = 0; k < nk; k++) {
+                float ms = 0.f;
+                XCG_CK(cudaEventElapsedTime(&ms, c->events[ei], c->events[ei + 1]), "cudaEventElapsedTime");
+                c->stats.kernel_ms[k] += ms;
+                ei += 2;
+            }
+    }
+    return XCG_OK;
+}
+
+xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m_ny,
+                         const void *slave, int32_t s_nx, int32_t s_ny,
+                         int32_t x_offset, int32_t y_offset, double astretcha,
+                         const xcg_loc *locs, int32_t nlocs, int32_t strip_len,
+                         xcg_result *results) {
+    if (!c || nlocs < 0 || (nlocs > 0 && (!master || !slave || !locs || !results))) return XCG_ERR_ARG;
+    if (m_nx <= 0 || m_ny <= 0 || s_nx <= 0 || s_ny <= 0) return XCG_ERR_ARG;
+    if (nlocs == 0) return XCG_OK;
+    XCG_CK(cudaSetDevice(c->device), "cudaSetDevice");
+    const size_t es = c->prm.format == 0 ? 4 : 4;   // int16 I/Q pair or float32
+    const size_t need[2] = {(size_t)m_nx * m_ny * es, (size_t)s_nx * s_ny * es};
+    for (int i = 0; i < 2; i++) {
+        if (need[i] > c->img_bytes[i]) {
+            cudaFree(c->d_img[i]);
+            c->d_img[i] = nullptr;
+            c->img_bytes[i] = 0;
+            XCG_CK(cudaMalloc(&c->d_img[i], need[i]), "cudaMalloc image");
+            c->img_bytes[i] = need[i];
+        }
+    }
+    if (nlocs > c->io_cap) {
+        cudaFree(c->d_locs); cudaFree(c->d_res);
+        c->d_locs = nullptr; c->d_res = nullptr; c->io_cap = 0;
+        XCG_CK(cudaMalloc(&c->d_locs, (size_t)nlocs * sizeof(xcg_loc)), "cudaMalloc locs");
+        XCG_CK(cudaMalloc(&c->d_res, (size_t)nlocs * sizeof(xcg_result)), "cudaMalloc results");
+        c->io_cap = nlocs;
+    }
+    cudaStream_t s = c->stream;
+    XCG_CK(cudaMemcpyAsync(c->d_img[0], master, need[0], cudaMemcpyHostToDevice, s), "copy master");
+    XCG_CK(cudaMemcpyAsync(c->d_img[1], slave, need[1], cudaMemcpyHostToDevice, s), "copy slave");
+    XCG_CK(cudaMemcpyAsync(c->d_locs, locs, (size_t)nlocs * sizeof(xcg_loc), cudaMemcpyHostToDevice, s), "copy locs");
+    xcg_status st = xcg_correlate_device(c, c->d_img[0], m_nx, m_ny, c->d_img[1], s_nx, s_ny, x_offset, y_offset,
+                                         astretcha, c->d_locs, nlocs, strip_len, c->d_res, (void *)s);
+    if (st != XCG_OK) return st;
+    XCG_CK(cudaMemcpyAsync(results, c->d_res, (size_t)nlocs * sizeof(xcg_result), cudaMemcpyDeviceToHost, s), "copy results");
+    XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    return XCG_OK;
+}
+
+}  // extern "C"

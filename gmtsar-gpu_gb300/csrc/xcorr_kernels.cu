@@ -1,0 +1,676 @@
+// The four kernels of the xcorr frequency-domain path on sm_103a.
+//
+//   k_rows   per 1024-sample chunk of rows: patch staging from the SLC
+//            images (int16 I/Q or float32), range interpolation, amplitude,
+//            the reference's FP32 chunk sums, and the forward row FFT of the
+//            packed real pair a1 + i*a2*mask.
+//   k_cols   per group of column pairs (kx, N-kx): forward column FFTs,
+//            Hermitian split into the two patch spectra, mean correction,
+//            conjugate product with the (-1)^(kx+ky) shift, inverse column FFT
+//            of the half spectrum kx <= N/2 for the surface rows only.
+//   k_peak   per window: inverse row FFTs (two real rows per complex FFT),
+//            |.| surface, integer argmax with the reference's tie rules,
+//            surface means, the int64 time-domain correlation at the peak,
+//            normalisation and the 8x8 neighbourhood ^0.25.
+//   k_subpix per window: separable zero-pad interpolation of the 8x8 block
+//            as two small dense operators and the argmax of the real part.
+//
+// Every kernel cites the reference stages it replaces.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "team_fft.cuh"
+#include "xcorr_kernels.cuh"
+
+namespace xcg {
+
+__host__ __device__ constexpr int team_lanes(int n) { return (n / 16 < 32) ? n / 16 : 32; }
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ unsigned bitrev11(unsigned e) { return __brev(e) >> 21; }
+
+// Sortable argmax key with the reference's tie rules (reduce6b / reduce6bC,
+// conv_ampl_demean.cu:227-346,434-554, host finish :655-673,739-754): a
+// thread starts from value 0 at the first element of its pair and takes a
+// later element only if strictly greater; tree levels keep the lower thread
+// on ties; the host keeps the earliest block.  Net effect: the winner has the
+// largest effective value, ties to the smallest (block, bit-reversed local
+// index); an element that is not > 0 counts as 0 in the first half of its
+// 2048-element block and never wins in the second half.
+__device__ __forceinline__ unsigned long long argmax_key(float v, unsigned e) {
+    const unsigned local = e & 2047u;
+    unsigned ord;
+    if (v > 0.f) ord = __float_as_uint(v) + 1u;
+    else ord = (local < 1024u) ? 1u : 0u;          // 0.0f -> 1, "never" -> 0
+    const unsigned key = ((e >> 11) << 11) | bitrev11(local);
+    return ((unsigned long long)ord << 32) | (0xffffffffu - key);
+}
+__device__ __forceinline__ unsigned argmax_index(unsigned long long k) {
+    const unsigned key = 0xffffffffu - (unsigned)(k & 0xffffffffu);
+    return ((key >> 11) << 11) | bitrev11(key & 2047u);
+}
+__device__ __forceinline__ float argmax_value(unsigned long long k) {
+    const unsigned ord = (unsigned)(k >> 32);
+    return ord <= 1u ? 0.f : __uint_as_float(ord - 1u);
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = u > v ? u : v;
+    }
+    return v;
+}
+__device__ __forceinline__ double warp_sum_f64(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ long long warp_sum_i64(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float2 load_sample(const Plan &P, const void *img, int nx, int ny, int x, int y, bool &oob) {
+    if (x < 0 || y < 0 || x >= nx || y >= ny) { oob = true; return make_float2(0.f, 0.f); }
+    const size_t i = (size_t)y * (size_t)nx + (size_t)x;
+    if (P.format == 0) {
+        const short2 s = __ldg(reinterpret_cast<const short2 *>(img) + i);
+        return make_float2((float)s.x, (float)s.y);
+    }
+    return make_float2(__ldg(reinterpret_cast<const float *>(img) + i), 0.f);
+}
+
+__device__ __forceinline__ int slave_row_shift(const Plan &P, int y) {
+    return (int)((double)y * P.astretcha);    // ishft, read_xcorr_data.c:65
+}
+
+// ---------------------------------------------------------------- k_rows
+// Replaces read_xcorr_data + the H2D patch cut (xcorr.cu:326-338), range
+// interpolation (xcorr.cu:237-250, fft_interpolate_routines.cu:76-113),
+// d_conv_ampl_strip (conv_ampl_demean.cu:98-108), h_reduceFD_strip (:703-726),
+// the demean/mask of d_mean_mask_strip (:111-139, applied in k_cols by
+// linearity) and the row half of the forward 2-D FFT (do_freq_xcorr.cu:99-101).
+//
+// Range interpolation: the reference pads the N-point spectrum to M = ri*N and
+// keeps fine samples m in [N/2, 3N/2).  Fine sample m = ri*q + p equals the
+// N-point inverse FFT of X[f]*exp(2 pi i f' p / M) / N at q (f' = f or f-N);
+// for p = 0 that is the input sample x[q] itself.  So one forward FFT and
+// ri-1 inverse FFTs of length N give every kept sample.
+template <int N>
+__global__ void __launch_bounds__(128) k_rows(Plan P) {
+    constexpr int T = team_lanes(N);
+    constexpr int TPW = 32 / T;
+    constexpr int PADN = fft_padded_len(N);
+    constexpr int RPC = (N >= 1024) ? 1 : 1024 / N;     // rows per 1024-sample chunk
+    constexpr int H = RPC / 2;
+    constexpr int ACC = (N >= 1024) ? 1024 : 512;
+    constexpr int TWL = fft_twiddle_len(N);
+    constexpr int PER = N / T;
+
+    extern __shared__ float4 smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
+    const int lane = l32 % T;
+    const int team = warp * TPW + l32 / T;
+    const int teams = blockDim.x / T;
+    char *tbase = reinterpret_cast<char *>(tw + TWL) +
+                  (size_t)team * (2 * PADN * sizeof(float2) + 2 * N * sizeof(float) + 2 * ACC * sizeof(float));
+    float2 *A = reinterpret_cast<float2 *>(tbase);
+    float2 *B = A + PADN;
+    float *rb = reinterpret_cast<float *>(B + PADN);    // [2][N]
+    float *acc = rb + 2 * N;                            // [2][ACC]
+
+    for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_row[i];
+    __syncthreads();
+
+    const int w = blockIdx.y;
+    const int c = blockIdx.x * teams + team;           // chunk (always < nchunks, see launcher)
+    const xcg_loc loc = P.locs[w];
+    const int npx = N, npy = P.npy;
+    const int x0[2] = {loc.x - npx / 2, loc.x + P.x_offset - npx / 2};
+    const int y0[2] = {loc.y - npy / 2, loc.y + P.y_offset + slave_row_shift(P, loc.y) - npy / 2};
+    const void *img[2] = {P.master, P.slave};
+    const int inx[2] = {P.m_nx, P.s_nx}, iny[2] = {P.m_ny, P.s_ny};
+    bool oob = false;
+    const int ri = P.ri, lg = P.log2ri;
+
+    for (int ir = 0; ir < RPC; ir++) {
+        const int r = c * RPC + ir;
+#pragma unroll 1
+        for (int pt = 0; pt < 2; pt++) {
+            float *row = rb + pt * N;
+            for (int k = lane; k < N; k += T)
+                A[fft_pad(k)] = load_sample(P, img[pt], inx[pt], iny[pt], x0[pt] + k, y0[pt] + r, oob);
+            __syncwarp();
+            if (ri == 1) {
+                for (int k = lane; k < N; k += T) {
+                    float2 v = A[fft_pad(k)];
+                    row[k] = hypotf(v.x, v.y);
+                }
+            } else {
+                for (int k = lane; k < N; k += T) {        // phase-0 samples are the input
+                    const int m = N / 2 + k;
+                    if ((m & (ri - 1)) == 0) {
+                        float2 v = A[fft_pad(m >> lg)];
+                        row[k] = hypotf(v.x, v.y);
+                    }
+                }
+                __syncwarp();
+                float2 *S = team_fft<N, -1>(A, B, tw, lane, T);
+                float2 sreg[PER];
+#pragma unroll
+                for (int i = 0; i < PER; i++) sreg[i] = S[fft_pad(lane + T * i)];
+                __syncwarp();
+#pragma unroll 1
+                for (int p = 1; p < ri; p++) {
+                    const float2 *ph = P.phase + (size_t)(p - 1) * N;
+#pragma unroll
+                    for (int i = 0; i < PER; i++) A[fft_pad(lane + T * i)] = cmulf(sreg[i], __ldg(ph + lane + T * i));
+                    __syncwarp();
+                    float2 *Y = team_fft<N, +1>(A, B, tw, lane, T);
+                    for (int k = lane; k < N; k += T) {
+                        const int m = N / 2 + k;
+                        if ((m & (ri - 1)) == p) {
+                            float2 v = Y[fft_pad(m >> lg)];
+                            row[k] = hypotf(v.x, v.y);
+                        }
+                    }
+                    __syncwarp();
+                }
+            }
+            __syncwarp();
+        }
+        // packed real pair and its row FFT; amplitudes for the time correlation
+        const bool rin = (r >= P.ysearch) && (r < npy - P.ysearch);
+        float *a1g = P.amp1 + ((size_t)w * npy + r) * npx;
+        const bool r2c = (r >= P.ysearch) && (r < P.ysearch + P.ny_corr);
+        float *a2g = P.amp2c + ((size_t)w * P.ny_corr + (r - P.ysearch)) * P.nx_corr;
+        for (int k = lane; k < N; k += T) {
+            const float a1 = rb[k], a2 = rb[N + k];
+            const bool in = rin && (k >= P.xsearch) && (k < npx - P.xsearch);
+            A[fft_pad(k)] = make_float2(a1, in ? a2 : 0.f);
+            a1g[k] = a1;
+            if (r2c && k >= P.xsearch && k < P.xsearch + P.nx_corr) a2g[k - P.xsearch] = a2;
+        }
+        __syncwarp();
+        float2 *Z = team_fft<N, -1>(A, B, tw, lane, T);
+        float2 *zg = P.zrow + ((size_t)w * npy + r) * npx;
+        for (int k = lane; k < N; k += T) zg[k] = Z[fft_pad(k)];
+        // chunk sums in the reference's order: x[t] + x[t+512] first
+#pragma unroll
+        for (int pt = 0; pt < 2; pt++) {
+            float *ac = acc + pt * ACC;
+            const float *row = rb + pt * N;
+            if (H == 0) {
+                for (int k = lane; k < N; k += T) ac[k] = row[k];
+            } else if (ir < H) {
+                for (int k = lane; k < N; k += T) ac[ir * N + k] = row[k];
+            } else {
+                for (int k = lane; k < N; k += T) ac[(ir - H) * N + k] = ac[(ir - H) * N + k] + row[k];
+            }
+        }
+        __syncwarp();
+    }
+    {   // any lane of the team that read outside an image
+        const unsigned tmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (l32 - lane));
+        oob = __any_sync(0xffffffffu, oob) && (__ballot_sync(0xffffffffu, oob) & tmask);
+    }
+    // remaining tree levels: strides ACC/2 .. 1 (ACC = 1024 only when a chunk is one row)
+#pragma unroll
+    for (int pt = 0; pt < 2; pt++) {
+        float *ac = acc + pt * ACC;
+        for (int st = ACC / 2; st >= 1; st >>= 1) {
+            for (int t = lane; t < st; t += T) ac[t] = ac[t] + ac[t + st];
+            __syncwarp();
+        }
+        if (lane == 0) P.part[((size_t)w * 2 + pt) * P.nchunks + c] = ac[0];
+    }
+    if (lane == 0) P.oobmap[(size_t)w * P.nchunks + c] = oob ? 1 : 0;
+}
+
+// ---------------------------------------------------------------- k_cols
+// Replaces the column half of the forward FFTs, d_mulaconjb/d_Cmul
+// (do_freq_xcorr.cu:32-64,106-109), the inverse FFT's column half and
+// d_scaleFft2D (:113-114), plus the patch means of h_reduceFD_strip
+// (conv_ampl_demean.cu:713-725) and the demean/mask of d_mean_mask_strip
+// (:111-139), applied here in the frequency domain: the master loses
+// m1*N*M at bin (0,0), the slave m2 times the DFT of its mask.
+template <int M>
+__global__ void __launch_bounds__(128) k_cols(Plan P) {
+    constexpr int T = team_lanes(M);
+    constexpr int PADM = fft_padded_len(M);
+    constexpr int CS = PADM + 1;
+    constexpr int CP = (M <= 256) ? 16 : (M == 512 ? 8 : 4);
+    constexpr int TWL = fft_twiddle_len(M);
+
+    extern __shared__ float4 smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *cols = tw + TWL;                   // [2*CP][CS]
+    const int teams = blockDim.x / T;
+    float2 *scratch = cols + 2 * CP * CS;      // [teams][PADM]
+    double *sh = reinterpret_cast<double *>(scratch + teams * PADM);   // m1, m2
+    float *pbuf = reinterpret_cast<float *>(sh + 2);                    // [2][nchunks]
+
+    const int w = blockIdx.y, b = blockIdx.x;
+    const int N = P.npx;
+    const int kx0 = b * CP;
+    const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
+    const int lane = l32 % T;
+    const int team = warp * (32 / T) + l32 / T;
+
+    for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_col[i];
+    for (int i = threadIdx.x; i < 2 * P.nchunks; i += blockDim.x) pbuf[i] = P.part[(size_t)w * 2 * P.nchunks + i];
+    for (int i = threadIdx.x; i < 2 * CP * M; i += blockDim.x) {
+        const int s = i % (2 * CP), row = i / (2 * CP);
+        int col;
+        if (s < CP) col = kx0 + s;
+        else { const int kx = kx0 + s - CP; col = (kx == 0) ? N / 2 : N - kx; }
+        cols[s * CS + fft_pad(row)] = P.zrow[((size_t)w * M + row) * N + col];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {                      // means in the reference's order (:719-724)
+        double s1 = 0.0, s2 = 0.0;
+        for (int i = 0; i < P.nchunks; i++) s1 += (double)pbuf[i];
+        for (int i = 0; i < P.nchunks; i++) s2 += (double)pbuf[P.nchunks + i];
+        s1 /= (double)(N * M);
+        s2 /= (double)(N * M);
+        sh[0] = s1; sh[1] = s2;
+        if (b == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
+    }
+    __syncthreads();
+    const float dc1 = (float)(sh[0] * (double)N * (double)M);
+    const float m2 = (float)sh[1];
+    float2 *scr = scratch + team * PADM;
+
+    for (int j = team; j < CP; j += teams) {
+        const int kx = kx0 + j;
+        float2 *a = cols + j * CS;
+        float2 *pa = cols + (CP + j) * CS;
+        float2 *ra = team_fft<M, -1>(a, scr, tw, lane, T);
+        if (ra != a) { for (int i = lane; i < M; i += T) a[fft_pad(i)] = ra[fft_pad(i)]; }
+        __syncwarp();
+        float2 *rp = team_fft<M, -1>(pa, scr, tw, lane, T);
+        if (rp != pa) { for (int i = lane; i < M; i += T) pa[fft_pad(i)] = rp[fft_pad(i)]; }
+        __syncwarp();
+        // the kx = 0 team also emits column N/2; the trip count stays warp-uniform
+        // because team_fft ends each pass with a full-warp __syncwarp
+        const int nout = __any_sync(0xffffffffu, kx == 0) ? 2 : 1;
+        for (int o = 0; o < nout; o++) {
+            // o = 0: column kx with partner pa (or itself for kx = 0); o = 1: column N/2, self-paired
+            const float2 *z = (o == 0) ? a : pa;
+            const float2 *zp = (o == 0) ? ((kx == 0) ? a : pa) : pa;
+            const int kxx = (o == 0) ? kx : N / 2;
+            const float2 bx = __ldg(P.box_x + kxx);
+            for (int ky = lane; ky < M; ky += T) {
+                const float2 z1 = z[fft_pad(ky)];
+                const float2 z2 = zp[fft_pad((M - ky) & (M - 1))];
+                // A1 = (z1 + conj z2)/2, A2 = (z1 - conj z2)/(2i)
+                float2 A1 = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+                float2 A2 = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+                if (kxx == 0 && ky == 0) A1.x -= dc1;
+                const float2 by = __ldg(P.box_y + ky);
+                const float2 bm = cmulf(bx, by);
+                A2.x -= m2 * bm.x;
+                A2.y -= m2 * bm.y;
+                float2 pr = cmulf_conj(A1, A2);
+                if ((kxx + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
+                scr[fft_pad(ky)] = pr;
+            }
+            __syncwarp();
+            float2 *dst = (o == 0) ? a : pa;
+            float2 *rq = team_fft<M, +1>(scr, dst, tw, lane, T);
+            if (rq != dst) { for (int i = lane; i < M; i += T) dst[fft_pad(i)] = rq[fft_pad(i)]; }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    // write rows y in [ysearch, ysearch+nyc) of the half spectrum, kx <= N/2
+    const int nslots = CP + (b == 0 ? 1 : 0);
+    for (int i = threadIdx.x; i < nslots * P.nyc; i += blockDim.x) {
+        const int s = i % nslots, yq = i / nslots;
+        const int kx = (s < CP) ? kx0 + s : N / 2;
+        const float2 v = cols[s * CS + fft_pad(yq + P.ysearch)];
+        P.qspec[((size_t)w * P.nyc + yq) * P.qpitch + kx] = v;
+    }
+}
+
+// ---------------------------------------------------------------- k_peak
+// Replaces the row half of the inverse FFT, d_fillcorrmat_strip/d_Cabs
+// (do_freq_xcorr.cu:26-29,67-84,141-143), h_reduce_strip (conv_ampl_demean.cu:642-675),
+// the per-window host loop of d_do_freq_corr_strip (do_freq_xcorr.cu:150-195),
+// the time correlation d_calc_time_corr_strip (do_time_int_xcorr.cu:71-100),
+// d_scaled_strip (conv_ampl_demean.cu:50-68) and d_cppow_strip (:75-95).
+template <int N>
+__global__ void __launch_bounds__(256) k_peak(Plan P) {
+    constexpr int T = team_lanes(N);
+    constexpr int PADN = fft_padded_len(N);
+    constexpr int TWL = fft_twiddle_len(N);
+    constexpr int NT = 256;
+
+    extern __shared__ float4 smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    const int teams = NT / T;
+    float2 *fb = tw + TWL;                                // [teams][2][PADN]
+    unsigned long long *rk = reinterpret_cast<unsigned long long *>(fb + teams * 2 * PADN);  // [8]
+    double *rd = reinterpret_cast<double *>(rk + 8);      // [2][8]
+    long long *ri64 = reinterpret_cast<long long *>(rd + 16);   // [3][8]
+    double *bc = reinterpret_cast<double *>(ri64 + 24);   // broadcast
+
+    const int w = blockIdx.x;
+    const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
+    const int lane = l32 % T;
+    const int team = warp * (32 / T) + l32 / T;
+    float2 *A = fb + team * 2 * PADN;
+    float2 *B = A + PADN;
+    const int M = P.npy, nxc = P.nxc, nyc = P.nyc;
+    const float scale = 1.0f / ((float)N * (float)M);
+
+    for (int i = threadIdx.x; i < TWL; i += NT) tw[i] = P.tw_row[i];
+    __syncthreads();
+
+    unsigned long long best = 0ull;
+    double hsum = 0.0, fsum = 0.0;
+    const float2 *q = P.qspec + (size_t)w * nyc * P.qpitch;
+    float *surf = P.surf + (size_t)w * nyc * nxc;
+    for (int pr = team; pr < nyc / 2; pr += teams) {
+        const int y1 = 2 * pr, y2 = y1 + 1;
+        for (int kx = lane; kx <= N / 2; kx += T) {
+            float2 q1 = q[(size_t)y1 * P.qpitch + kx], q2 = q[(size_t)y2 * P.qpitch + kx];
+            if (kx == 0 || kx == N / 2) { q1.y = 0.f; q2.y = 0.f; }
+            A[fft_pad(kx)] = make_float2(q1.x - q2.y, q1.y + q2.x);
+            if (kx > 0 && kx < N / 2) A[fft_pad(N - kx)] = make_float2(q1.x + q2.y, q2.x - q1.y);
+        }
+        __syncwarp();
+        const float2 *R = team_fft<N, +1>(A, B, tw, lane, T);
+        for (int xq = lane; xq < nxc; xq += T) {
+            const float2 v = R[fft_pad(xq + P.nx_corr / 2)];
+            const float c1 = fabsf(v.x * scale), c2 = fabsf(v.y * scale);
+            surf[(size_t)y1 * nxc + xq] = c1;
+            surf[(size_t)y2 * nxc + xq] = c2;
+            const unsigned e1 = (unsigned)(y1 * nxc + xq), e2 = (unsigned)(y2 * nxc + xq);
+            unsigned long long k1 = argmax_key(c1, e1), k2 = argmax_key(c2, e2);
+            best = k1 > best ? k1 : best;
+            best = k2 > best ? k2 : best;
+            fsum += (double)c1 + (double)c2;
+            if (!(e1 & 512u)) hsum += (double)c1;      // reduce6<double,1024> keeps local [0,512) and [1024,1536)
+            if (!(e2 & 512u)) hsum += (double)c2;
+        }
+        __syncwarp();
+    }
+    best = warp_max_u64(best);
+    hsum = warp_sum_f64(hsum);
+    fsum = warp_sum_f64(fsum);
+    if (l32 == 0) { rk[warp] = best; rd[warp] = hsum; rd[8 + warp] = fsum; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long bb = rk[0];
+        double hs = rd[0], fs = rd[8];
+        for (int i = 1; i < NT / 32; i++) { bb = rk[i] > bb ? rk[i] : bb; hs += rd[i]; fs += rd[8 + i]; }
+        rk[0] = bb; rd[0] = hs; rd[8] = fs;
+    }
+    __syncthreads();
+    const unsigned pk = argmax_index(rk[0]);
+    const int ip = (int)(pk / (unsigned)nxc), jp = (int)(pk % (unsigned)nxc);
+    const double cmax = (double)argmax_value(rk[0]);
+    const float jpeak = (float)jp - (float)nxc / 2.0f;     // do_freq_xcorr.cu:158-159
+    const float ipeak = (float)ip - (float)nyc / 2.0f;
+
+    // time-domain correlation at the integer peak on (int) demeaned amplitudes
+    const float m1f = (float)P.means[2 * w], m2f = (float)P.means[2 * w + 1];
+    const float *a1 = P.amp1 + (size_t)w * M * N + (size_t)(P.ysearch + (int)ipeak) * N + (int)jpeak + P.xsearch;
+    const float *a2 = P.amp2c + (size_t)w * P.ny_corr * P.nx_corr;
+    long long sn = 0, s1 = 0, s2 = 0;
+    for (int i = threadIdx.x; i < P.ny_corr * P.nx_corr; i += NT) {
+        const int r = i / P.nx_corr, cc = i - r * P.nx_corr;
+        float va = a1[(size_t)r * N + cc] - m1f;
+        va = va * 1.0f;
+        float vb = a2[i] - m2f;
+        vb = vb * 1.0f;
+        const long long ia = (long long)(int)va, ib = (long long)(int)vb;
+        sn += ia * ib; s1 += ia * ia; s2 += ib * ib;
+    }
+    sn = warp_sum_i64(sn); s1 = warp_sum_i64(s1); s2 = warp_sum_i64(s2);
+    if (l32 == 0) { ri64[warp] = sn; ri64[8 + warp] = s1; ri64[16 + warp] = s2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long tn = 0, t1 = 0, t2 = 0;
+        for (int i = 0; i < NT / 32; i++) { tn += ri64[i]; t1 += ri64[8 + i]; t2 += ri64[16 + i]; }
+        const double gd = sqrt(1.0 * (double)t1 * (double)t2);
+        const double gamma = (gd == 0.0) ? 0.0 : 100.0 * fabs((double)tn / gd);
+        const double msc = cmax / gamma;
+        bc[0] = gamma;
+        bc[1] = msc;
+        const double c0n = (double)surf[0] / msc;
+        P.corr0n[w] = c0n;
+        xcg_result &o = P.out[w];
+        o.xoff = -1 * jpeak;
+        o.yoff = -1 * ipeak;
+        o.corr = (float)gamma;
+        o.ip = ip; o.jp = jp;
+        int fl = 0;
+        for (int i = 0; i < P.nchunks; i++) fl |= P.oobmap[(size_t)w * P.nchunks + i] ? XCG_FLAG_OOB : 0;
+        o.flags = fl;
+        o.cmax = cmax;
+        o.cave = rd[0] / (double)(nxc * nyc);
+        o.cave_true = rd[8] / (double)(nxc * nyc);
+        o.gamma = gamma;
+        o.mean1 = P.means[2 * w];
+        o.mean2 = P.means[2 * w + 1];
+        o.corr0n = c0n;
+        o.fip = -1; o.fjp = -1; o.fmax = 0.f; o.xfrac = 0.f; o.yfrac = 0.f;
+    }
+    __syncthreads();
+    // 8x8 neighbourhood with the reference's flat bounds test (conv_ampl_demean.cu:82-93)
+    if (P.interp_flag) {
+        const int n2 = P.n2x * P.n2y;
+        const double msc = bc[1];
+        const int jc = (nxc / 2) - P.n2x / 2 - (int)(-1 * jpeak);
+        const int ic = (nyc / 2) - P.n2y / 2 - (int)(-1 * ipeak);
+        const long long ns = (long long)nxc * nyc;
+        for (int t = threadIdx.x; t < n2; t += NT) {
+            const int iy = t / P.n2x, ix = t - iy * P.n2x;
+            const long long k = (long long)(ic + iy) * nxc + (jc + ix);
+            float v = 0.f;
+            unsigned char nx = 0;
+            if (k >= 0 && k < ns) v = powf((float)((double)surf[k] / msc), 0.25f);
+            else if (k == ns) nx = 1;
+            P.md[(size_t)w * n2 + t] = v;
+            P.mdnext[(size_t)w * n2 + t] = nx;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- k_subpix
+// Replaces d_do_highres_corr (highres_corr.cu:23-79): the 2-D zero-pad
+// interpolation d_fft_interpolate_2d_strip (fft_interpolate_routines.cu:118-147)
+// as out = KY * md * KX^T with KX (nx2 x n2x) and KY (ny2 x n2y) the exact
+// FFT-pad-IFFT-scale operators, then the argmax of the real part
+// (h_reduceCr_strip, conv_ampl_demean.cu:730-756) and the fractions
+// (highres_corr.cu:59-76).
+__global__ void __launch_bounds__(256) k_subpix(Plan P) {
+    extern __shared__ float4 smem_raw[];
+    const int n2x = P.n2x, n2y = P.n2y, nx2 = P.nx2, ny2 = P.ny2;
+    float *md = reinterpret_cast<float *>(smem_raw);                 // [n2y*n2x]
+    float2 *tr = reinterpret_cast<float2 *>(md + 64);                // [n2y][nx2]
+    float2 *kys = tr + n2y * nx2;                                    // [ny2][n2y]
+    unsigned long long *rk = reinterpret_cast<unsigned long long *>(kys + ny2 * n2y);
+    int *fl = reinterpret_cast<int *>(rk + 8);
+
+    const int w = blockIdx.x;
+    const int n2 = n2x * n2y;
+    if (threadIdx.x == 0) *fl = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+        float v = P.md[(size_t)w * n2 + t];
+        if (P.mdnext[(size_t)w * n2 + t]) {
+            const int g = P.win0 + w + 1;    // the reference reads the next window of its strip
+            const bool same = P.strip_len > 0 && g < P.nlocs_total && (g % P.strip_len) != 0 && (w + 1) < P.nwin;
+            v = same ? powf((float)P.corr0n[w + 1], 0.25f) : 0.f;
+            atomicOr(fl, XCG_FLAG_NEXTREAD);
+        }
+        md[t] = v;
+    }
+    for (int t = threadIdx.x; t < ny2 * n2y; t += blockDim.x) kys[t] = __ldg(P.ky + t);
+    __syncthreads();
+    // row pass: tr[r][X] = sum_c md[r][c] * KX[X][c]
+    for (int t = threadIdx.x; t < n2y * nx2; t += blockDim.x) {
+        const int r = t / nx2, X = t - r * nx2;
+        float2 s = make_float2(0.f, 0.f);
+        for (int c = 0; c < n2x; c++) {
+            const float2 k = __ldg(P.kx + X * n2x + c);
+            const float m = md[r * n2x + c];
+            s.x = fmaf(m, k.x, s.x);
+            s.y = fmaf(m, k.y, s.y);
+        }
+        tr[t] = s;
+    }
+    __syncthreads();
+    // column pass, real part only, and the argmax
+    unsigned long long best = 0ull;
+    for (int e = threadIdx.x; e < ny2 * nx2; e += blockDim.x) {
+        const int Y = e / nx2, X = e - Y * nx2;
+        float re = 0.f;
+        for (int r = 0; r < n2y; r++) {
+            const float2 k = kys[Y * n2y + r], t = tr[r * nx2 + X];
+            re = fmaf(k.x, t.x, re);
+            re = fmaf(-k.y, t.y, re);
+        }
+        const unsigned long long kk = argmax_key(re, (unsigned)e);
+        best = kk > best ? kk : best;
+    }
+    best = warp_max_u64(best);
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) rk[warp] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long bb = rk[0];
+        for (int i = 1; i < (int)(blockDim.x >> 5); i++) bb = rk[i] > bb ? rk[i] : bb;
+        const unsigned pk = argmax_index(bb);
+        const int fip = (int)(pk / (unsigned)nx2), fjp = (int)(pk % (unsigned)nx2);
+        xcg_result &o = P.out[w];
+        o.fip = fip;
+        o.fjp = fjp;
+        o.fmax = argmax_value(bb);
+        const float jpeak = (float)fjp - (float)ny2 / 2.0f;    // ny2 for both axes (highres_corr.cu:61-62)
+        const float ipeak = (float)fip - (float)ny2 / 2.0f;
+        o.xfrac = jpeak / (float)P.ifc;
+        o.yfrac = ipeak / (float)P.ifc;
+        o.flags |= *fl;
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+
+template <int N>
+static size_t rows_smem() {
+    constexpr int T = team_lanes(N);
+    constexpr int ACC = (N >= 1024) ? 1024 : 512;
+    const int teams = 128 / T;
+    return fft_twiddle_len(N) * sizeof(float2) +
+           (size_t)teams * (2 * fft_padded_len(N) * sizeof(float2) + 2 * N * sizeof(float) + 2 * ACC * sizeof(float));
+}
+template <int M>
+static size_t cols_smem(int nchunks) {
+    constexpr int T = team_lanes(M);
+    constexpr int CP = (M <= 256) ? 16 : (M == 512 ? 8 : 4);
+    const int teams = 128 / T;
+    return fft_twiddle_len(M) * sizeof(float2) + (size_t)2 * CP * (fft_padded_len(M) + 1) * sizeof(float2) +
+           (size_t)teams * fft_padded_len(M) * sizeof(float2) + 2 * sizeof(double) + 2 * nchunks * sizeof(float);
+}
+template <int N>
+static size_t peak_smem() {
+    constexpr int T = team_lanes(N);
+    const int teams = 256 / T;
+    return fft_twiddle_len(N) * sizeof(float2) + (size_t)teams * 2 * fft_padded_len(N) * sizeof(float2) +
+           8 * sizeof(unsigned long long) + 16 * sizeof(double) + 24 * sizeof(long long) + 4 * sizeof(double);
+}
+static size_t subpix_smem(const Plan &P) {
+    return 64 * sizeof(float) + (size_t)P.n2y * P.nx2 * sizeof(float2) + (size_t)P.ny2 * P.n2y * sizeof(float2) +
+           8 * sizeof(unsigned long long) + 16;
+}
+
+template <int N>
+static cudaError_t setup_rows() {
+    return cudaFuncSetAttribute(k_rows<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>());
+}
+template <int M>
+static cudaError_t setup_cols(int nchunks) {
+    return cudaFuncSetAttribute(k_cols<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<M>(nchunks));
+}
+template <int N>
+static cudaError_t setup_peak() {
+    return cudaFuncSetAttribute(k_peak<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)peak_smem<N>());
+}
+
+cudaError_t kernels_setup(const Plan &P) {
+    cudaError_t e = cudaSuccess;
+    switch (P.npx) {
+        case 128: e = setup_rows<128>(); if (!e) e = setup_peak<128>(); break;
+        case 256: e = setup_rows<256>(); if (!e) e = setup_peak<256>(); break;
+        case 512: e = setup_rows<512>(); if (!e) e = setup_peak<512>(); break;
+        case 1024: e = setup_rows<1024>(); if (!e) e = setup_peak<1024>(); break;
+        default: return cudaErrorInvalidValue;
+    }
+    if (e) return e;
+    switch (P.npy) {
+        case 128: e = setup_cols<128>(P.nchunks); break;
+        case 256: e = setup_cols<256>(P.nchunks); break;
+        case 512: e = setup_cols<512>(P.nchunks); break;
+        case 1024: e = setup_cols<1024>(P.nchunks); break;
+        default: return cudaErrorInvalidValue;
+    }
+    if (e) return e;
+    return cudaFuncSetAttribute(k_subpix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)subpix_smem(P));
+}
+
+template <int N>
+static void launch_rows_t(const Plan &P, cudaStream_t s) {
+    const int teams = 128 / team_lanes(N);
+    dim3 grid(P.nchunks / teams, P.nwin);
+    k_rows<N><<<grid, 128, rows_smem<N>(), s>>>(P);
+}
+template <int M>
+static void launch_cols_t(const Plan &P, cudaStream_t s) {
+    constexpr int CP = (M <= 256) ? 16 : (M == 512 ? 8 : 4);
+    dim3 grid((P.npx / 2) / CP, P.nwin);
+    k_cols<M><<<grid, 128, cols_smem<M>(P.nchunks), s>>>(P);
+}
+template <int N>
+static void launch_peak_t(const Plan &P, cudaStream_t s) {
+    k_peak<N><<<P.nwin, 256, peak_smem<N>(), s>>>(P);
+}
+
+void launch_rows(const Plan &P, cudaStream_t s) {
+    switch (P.npx) {
+        case 128: launch_rows_t<128>(P, s); break;
+        case 256: launch_rows_t<256>(P, s); break;
+        case 512: launch_rows_t<512>(P, s); break;
+        case 1024: launch_rows_t<1024>(P, s); break;
+    }
+}
+void launch_cols(const Plan &P, cudaStream_t s) {
+    switch (P.npy) {
+        case 128: launch_cols_t<128>(P, s); break;
+        case 256: launch_cols_t<256>(P, s); break;
+        case 512: launch_cols_t<512>(P, s); break;
+        case 1024: launch_cols_t<1024>(P, s); break;
+    }
+}
+void launch_peak(const Plan &P, cudaStream_t s) {
+    switch (P.npx) {
+        case 128: launch_peak_t<128>(P, s); break;
+        case 256: launch_peak_t<256>(P, s); break;
+        case 512: launch_peak_t<512>(P, s); break;
+        case 1024: launch_peak_t<1024>(P, s); break;
+    }
+}
+void launch_subpix(const Plan &P, cudaStream_t s) {
+    k_subpix<<<P.nwin, 256, subpix_smem(P), s>>>(P);
+}
+
+}  // namespace xcg

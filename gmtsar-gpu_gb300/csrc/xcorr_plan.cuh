@@ -1,0 +1,61 @@
+// Device-side plan shared by the xcorr kernels: sizes, image views, tables
+// and the per-batch scratch layout.  Passed to every kernel by value.
+#pragma once
+#include <stdint.h>
+
+#include "xcorr_gb300.h"
+
+namespace xcg {
+
+struct Plan {
+    // geometry (parse_xcorr_input.c:67-86)
+    int npx, npy;          // patch: 4*xsearch x 4*ysearch
+    int nxc, nyc;          // surface: 2*xsearch x 2*ysearch
+    int nx_corr, ny_corr;  // time-correlation window
+    int xsearch, ysearch;
+    int ri, log2ri;
+    int interp_flag, ifc, n2x, n2y, nx2, ny2;
+    int format;            // 0 complex int16, 1 float32 real
+    int nchunks;           // 1024-sample chunks per patch (npx*npy/1024)
+    int qpitch;            // row pitch (complex) of the half-spectrum rows: npx/2 + 16
+
+    // images
+    const void *master;
+    int m_nx, m_ny;
+    const void *slave;
+    int s_nx, s_ny;
+    int x_offset, y_offset;
+    double astretcha;
+
+    // windows of this batch
+    const xcg_loc *locs;   // already offset to the batch's first window
+    int nwin;              // windows in this batch
+    int strip_len;         // 0: no cross-window read
+    int win0;              // global index of the batch's first window
+    int nlocs_total;
+    xcg_result *out;       // offset to the batch's first window
+
+    // tables (device, built on the host in double)
+    const float2 *tw_row;   // Stockham twiddles for npx
+    const float2 *tw_col;   // Stockham twiddles for npy
+    const float2 *phase;    // (ri-1) x npx: exp(+2 pi i f' p / (ri npx)) / npx
+    const float2 *box_x;    // npx: DFT of the column mask
+    const float2 *box_y;    // npy: DFT of the row mask
+    const float2 *kx;       // nx2 x n2x interpolation operator (row pass)
+    const float2 *ky;       // ny2 x n2y (column pass)
+
+    // scratch (per batch, indexed by batch-local window)
+    float2 *zrow;     // [nwin][npy][npx]   row spectra of a1 + i*a2*mask
+    float *amp1;      // [nwin][npy][npx]   master amplitudes
+    float *amp2c;     // [nwin][ny_corr][nx_corr] slave amplitudes, centre
+    float *part;      // [nwin][2][nchunks] FP32 chunk sums (master, slave)
+    unsigned char *oobmap;  // [nwin][nchunks] 1 where a chunk read outside its image
+    double *means;    // [nwin][2]
+    float2 *qspec;    // [nwin][nyc][qpitch] column-inverted half spectrum
+    float *surf;      // [nwin][nyc][nxc]  correlation surface
+    float *md;        // [nwin][n2y*n2x]  neighbourhood ^0.25, NaN-safe
+    unsigned char *mdnext;  // [nwin][n2y*n2x] 1 where the next window's value goes
+    double *corr0n;   // [nwin]
+};
+
+}  // namespace xcg

@@ -1,1 +1,174 @@
-"""xcorr_gb300: Python binding of the GB300 xcorr library (placeholder, filled in below)."""
+"""ctypes binding of libxcorr_gb300.so (the C ABI in include/xcorr_gb300.h).
+
+This module only marshals arguments: every computation runs in the CUDA
+library.  Loading fails loudly when the library is missing; there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+LIB_PATH = os.path.join(_PKG, "lib", "libxcorr_gb300.so")
+
+XCG_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "unsupported", 3: "CUDA error", 4: "out of memory",
+          5: "no usable CUDA device", 6: "size exceeds a fixed limit"}
+FLAG_OOB = 1
+FLAG_NEXTREAD = 2
+
+# every entry point include/xcorr_gb300.h declares
+EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_create", "xcg_destroy",
+           "xcg_correlate", "xcg_correlate_device", "xcg_set_profiling", "xcg_get_stats")
+
+
+class Params(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in
+                ("xsearch", "ysearch", "nx_corr", "ny_corr", "ri", "interp_flag", "interp_factor",
+                 "n2x", "n2y", "format")]
+
+
+class Loc(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_int32), ("y", ctypes.c_int32)]
+
+
+RESULT_DTYPE = np.dtype([
+    ("xoff", "<f4"), ("yoff", "<f4"), ("xfrac", "<f4"), ("yfrac", "<f4"), ("corr", "<f4"),
+    ("ip", "<i4"), ("jp", "<i4"), ("fip", "<i4"), ("fjp", "<i4"), ("flags", "<i4"),
+    ("fmax", "<f4"),
+    ("cmax", "<f8"), ("cave", "<f8"), ("cave_true", "<f8"), ("gamma", "<f8"),
+    ("mean1", "<f8"), ("mean2", "<f8"), ("corr0n", "<f8"),
+], align=True)
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_int64), ("batches", ctypes.c_int32), ("batch_windows", ctypes.c_int32),
+                ("kernel_ms", ctypes.c_double * 4), ("scratch_bytes", ctypes.c_size_t)]
+
+
+KERNEL_NAMES = ("k_rows", "k_cols", "k_peak", "k_subpix")
+
+_lib = None
+
+
+class XcgError(RuntimeError):
+    pass
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (build it first with gmtsar-gpu_gb300/build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise XcgError(f"libxcorr_gb300.so not found at {path}; run gmtsar-gpu_gb300/build.py")
+    L = ctypes.CDLL(path)
+    L.xcg_status_string.restype = ctypes.c_char_p
+    L.xcg_status_string.argtypes = [ctypes.c_int]
+    L.xcg_last_error.restype = ctypes.c_char_p
+    L.xcg_default_params.argtypes = [ctypes.POINTER(Params)]
+    L.xcg_create.restype = ctypes.c_int
+    L.xcg_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
+    L.xcg_destroy.argtypes = [ctypes.c_void_p]
+    L.xcg_correlate.restype = ctypes.c_int
+    L.xcg_correlate.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]
+    L.xcg_correlate_device.restype = ctypes.c_int
+    L.xcg_correlate_device.argtypes = L.xcg_correlate.argtypes + [ctypes.c_void_p]
+    L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    L.xcg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != XCG_OK:
+        L = load()
+        raise XcgError(f"{L.xcg_status_string(rc).decode()}: {L.xcg_last_error().decode()}")
+
+
+def params(xsearch=64, ysearch=64, ri=2, interp_flag=1, interp_factor=16, fmt=0) -> Params:
+    """Parameters derived the way parse_xcorr_input.c:139-158 couples them."""
+    return Params(xsearch=xsearch, ysearch=ysearch, nx_corr=2 * xsearch, ny_corr=2 * ysearch, ri=ri,
+                  interp_flag=interp_flag, interp_factor=interp_factor, n2x=8, n2y=8, format=fmt)
+
+
+class Context:
+    """One correlation context (xcg_create ... xcg_destroy)."""
+
+    def __init__(self, p: Params, device: int = 0, max_batch: int = 0):
+        self._L = load()
+        self.params = p
+        h = ctypes.c_void_p()
+        _check(self._L.xcg_create(ctypes.byref(p), device, max_batch, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._L.xcg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_profiling(self, on: bool):
+        self._L.xcg_set_profiling(self._h, 1 if on else 0)
+
+    def stats(self) -> Stats:
+        s = Stats()
+        self._L.xcg_get_stats(self._h, ctypes.byref(s))
+        return s
+
+    def correlate(self, master: np.ndarray, slave: np.ndarray, locs: np.ndarray, x_offset=0, y_offset=0,
+                  astretcha=0.0, strip_len=0) -> np.ndarray:
+        """Host arrays in, host results out.  master/slave: (ny, nx, 2) int16 or (ny, nx) float32."""
+        master = np.ascontiguousarray(master)
+        slave = np.ascontiguousarray(slave)
+        locs = np.ascontiguousarray(locs, dtype=np.int32).reshape(-1, 2)
+        out = np.zeros(len(locs), dtype=RESULT_DTYPE)
+        _check(self._L.xcg_correlate(self._h, master.ctypes.data, master.shape[1], master.shape[0],
+                                     slave.ctypes.data, slave.shape[1], slave.shape[0],
+                                     int(x_offset), int(y_offset), float(astretcha),
+                                     locs.ctypes.data, len(locs), int(strip_len), out.ctypes.data))
+        return out
+
+    def correlate_device(self, d_master: int, m_nx: int, m_ny: int, d_slave: int, s_nx: int, s_ny: int,
+                         d_locs: int, nlocs: int, d_results: int, stream: int = 0, x_offset=0, y_offset=0,
+                         astretcha=0.0, strip_len=0):
+        """Device pointers in and out (integers), enqueued on `stream`."""
+        _check(self._L.xcg_correlate_device(self._h, d_master, m_nx, m_ny, d_slave, s_nx, s_ny,
+                                            int(x_offset), int(y_offset), float(astretcha),
+                                            d_locs, nlocs, int(strip_len), d_results, stream))
+
+
+def grid(m_nx, m_ny, nxl, nyl, xsearch=64, ysearch=64):
+    """Location grid of get_locations.c:21-40 (npx = 4*xsearch, nx_corr = 2*xsearch)."""
+    npx, npy = 4 * xsearch, 4 * ysearch
+    x_inc = (m_nx - 2 * (xsearch + 2 * xsearch)) // (nxl + 3)
+    y_inc = (m_ny - 2 * (ysearch + 2 * ysearch)) // (nyl + 1)
+    return np.array([(npx + i * x_inc, npy + j * y_inc)
+                     for j in range(1, nyl + 1) for i in range(2, nxl + 2)], np.int32)
+
+
+def output_offsets(res, ri, x_offset, y_offset, locs_y, astretcha):
+    """The offsets print_results writes (print_results.c:30-38), in float32."""
+    f = np.float32
+    ishft = np.trunc(np.asarray(locs_y, np.float64) * astretcha).astype(np.int32)
+    xo = (res["xoff"].astype(f) / f(ri)) - (res["xfrac"].astype(f) / f(ri)) + f(x_offset)
+    yo = res["yoff"].astype(f) - res["yfrac"].astype(f) + f(y_offset) + ishft.astype(f)
+    return xo.astype(f), yo.astype(f)

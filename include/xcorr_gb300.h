@@ -1,0 +1,129 @@
+/* xcorr_gb300: GB300 (sm_103a) implementation of GMTSAR's xcorr
+ * frequency-domain patch-offset estimator, behind a plain C ABI.
+ *
+ * One call correlates a list of locations between a master and an aligned
+ * (slave) SLC image and returns, per location, the fields of the reference's
+ * `struct locs` (xcorr.h:6-17) plus the reduction diagnostics.  It replaces
+ * the reference's `do_correlation(struct xcorr)` (xcorr.cu:299-378) together
+ * with the stages it drives: range interpolation and amplitude/demean
+ * (xcorr.cu:237-292), do_freq_xcorr (do_freq_xcorr.cu:123-200),
+ * do_time_int_xcorr's GPU score (do_time_int_xcorr.cu:71-100) and
+ * highres_corr (highres_corr.cu:23-79).  Errors come back as status codes
+ * instead of exit() (gpu_err.h:13-32).
+ *
+ * Threading: a context may be used by one host thread at a time.
+ */
+#ifndef XCORR_GB300_H
+#define XCORR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    XCG_OK = 0,
+    XCG_ERR_ARG = 1,          /* bad argument or parameter combination */
+    XCG_ERR_UNSUPPORTED = 2,  /* valid for the reference but not built here */
+    XCG_ERR_CUDA = 3,         /* a CUDA runtime call failed (see xcg_last_error) */
+    XCG_ERR_NOMEM = 4,        /* device or pinned allocation failed */
+    XCG_ERR_NO_DEVICE = 5,    /* no CUDA device / extension cannot run */
+    XCG_ERR_TOO_LARGE = 6     /* a size exceeds a fixed limit */
+} xcg_status;
+
+/* Correlation parameters (struct xcorr fields, xcorr.h:19-63, with the
+ * defaults of set_defaults, parse_xcorr_input.c:38-88). */
+typedef struct {
+    int32_t xsearch, ysearch;   /* search half-widths, powers of two in 32..256 (default 64) */
+    int32_t nx_corr, ny_corr;   /* correlation window; the reference ties them to 2*xsearch, 2*ysearch */
+    int32_t ri;                 /* range interpolation factor: 1 (-norange), 2 (default), 4 or 8 */
+    int32_t interp_flag;        /* 1: subpixel refinement (default); 0: -nointerp */
+    int32_t interp_factor;      /* subpixel factor: 8, 16 (default) or 32 */
+    int32_t n2x, n2y;           /* peak neighbourhood, 8 x 8 (parse_xcorr_input.c:75-76) */
+    int32_t format;             /* 0: complex int16 I/Q samples; 1: float32 real samples (-real) */
+} xcg_params;
+
+/* A location: master pixel (range x, azimuth y) of the window centre,
+ * struct locs x/y (xcorr.h:7-8) as get_locations (get_locations.c:29-40) sets them. */
+typedef struct {
+    int32_t x, y;
+} xcg_loc;
+
+enum { XCG_FLAG_OOB = 1,        /* part of a patch fell outside its image and was zero-filled */
+       XCG_FLAG_NEXTREAD = 2 }; /* the 8x8 neighbourhood used the next window's first surface value */
+
+/* Per-location result. */
+typedef struct {
+    float xoff, yoff;    /* integer offset = -(peak - surface centre), struct locs xoff/yoff */
+    float xfrac, yfrac;  /* subpixel fraction, struct locs xfrac/yfrac */
+    float corr;          /* time-domain correlation at the integer peak (percent), struct locs corr */
+    int32_t ip, jp;      /* integer peak row/column in the nyc x nxc surface */
+    int32_t fip, fjp;    /* subpixel peak row/column in the interpolated surface (-1 if none) */
+    int32_t flags;       /* XCG_FLAG_* */
+    float fmax;          /* interpolated peak value (real part) */
+    double cmax;         /* surface maximum */
+    double cave;         /* the reference's surface mean (half-block sums / count) */
+    double cave_true;    /* mean over the whole surface */
+    double gamma;        /* time-domain correlation in double */
+    double mean1, mean2; /* patch amplitude means, master and slave */
+    double corr0n;       /* normalised surface value at lag (-xsearch, -ysearch) */
+} xcg_result;
+
+typedef struct xcg_ctx xcg_ctx;
+
+/* Kernel timing/launch statistics of the most recent correlate call. */
+typedef struct {
+    int64_t launches;          /* kernels launched by this library */
+    int32_t batches;
+    int32_t batch_windows;     /* windows per batch */
+    double kernel_ms[4];       /* rows, columns, peak, subpixel: summed CUDA-event time when profiling */
+    size_t scratch_bytes;      /* device scratch held by the context */
+} xcg_stats;
+
+const char *xcg_status_string(xcg_status s);
+/* Message of the last CUDA error seen by this thread. */
+const char *xcg_last_error(void);
+
+/* Fill p with the reference defaults (xsearch=ysearch=64, ri=2, interp 16). */
+void xcg_default_params(xcg_params *p);
+
+/* Create a context on `device`: validates p, builds the transform tables and
+ * allocates scratch for up to `max_batch` windows per launch (0: automatic). */
+xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xcg_ctx **out);
+void xcg_destroy(xcg_ctx *ctx);
+
+/* Correlate `nlocs` locations; all buffers are HOST memory.
+ * master: m_ny lines of m_nx samples (format 0: int16 I,Q pairs; 1: float32).
+ * x_offset/y_offset: rshift/ashift of the aligned PRM; astretcha: (prf2-prf1)/prf1.
+ * The slave window of location (x,y) starts at x + x_offset - npx/2,
+ * y + y_offset + (int)(y*astretcha) - npy/2 (read_xcorr_data.c:65-75, xcorr.cu:332-333).
+ * strip_len: locations per strip (nxl) for the one cross-window read the
+ * reference makes; 0 disables it.  Synchronous. */
+xcg_status xcg_correlate(xcg_ctx *ctx,
+                         const void *master, int32_t m_nx, int32_t m_ny,
+                         const void *slave, int32_t s_nx, int32_t s_ny,
+                         int32_t x_offset, int32_t y_offset, double astretcha,
+                         const xcg_loc *locs, int32_t nlocs, int32_t strip_len,
+                         xcg_result *results);
+
+/* Same with DEVICE pointers (images, locations, results), enqueued on
+ * `stream` (a cudaStream_t, NULL for the legacy stream); returns after the
+ * launches are enqueued. */
+xcg_status xcg_correlate_device(xcg_ctx *ctx,
+                                const void *d_master, int32_t m_nx, int32_t m_ny,
+                                const void *d_slave, int32_t s_nx, int32_t s_ny,
+                                int32_t x_offset, int32_t y_offset, double astretcha,
+                                const xcg_loc *d_locs, int32_t nlocs, int32_t strip_len,
+                                xcg_result *d_results, void *stream);
+
+/* Record CUDA events around every kernel launch (adds a synchronisation at
+ * the end of each correlate call to read them). */
+void xcg_set_profiling(xcg_ctx *ctx, int32_t enable);
+void xcg_get_stats(const xcg_ctx *ctx, xcg_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XCORR_GB300_H */
