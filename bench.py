@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Benchmark of the xcorr patch-offset path on GB300: windows/s.
+
+Workload (one "step"): the 128x128-window configuration, a synthetic
+complex-int16 speckle pair of 2048 (range) x 4096 (azimuth) samples with the
+slave shifted by (+3.37, -5.81) px and 10% noise, 20 x 50 = 1000 locations,
+xsearch = ysearch = 64 (256 x 256 FFTs), range_interp 2, subpixel factor 16,
+FP32.  Every step runs the whole path over the 1000 windows.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value: windows/s with the images resident in HBM, timed per step with CUDA
+events on the launching stream; L2 (129 MB; the image pair is 64 MB) is
+flushed by writing a 256 MB buffer before every step, outside the events.
+e2e: the same metric through the host-buffer C entry point (xcg_correlate),
+pinned host images copied in and results copied back inside every step.
+--impl reference: the CPU restatement of the reference path (oracle/, all host
+cores), the only CPU implementation of this path there is.
+Under torchrun (N > 1) every rank correlates its own copy of the workload
+(windows are independent: weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "gmtsar-gpu_gb300", "python"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "xcorr windows/s at 128^2 (plain FFT-interpolation form)"
+UNIT = "windows/s"
+WORKLOAD = dict(workload="xcorr plain path, 128x128 windows (256x256 FFT)", image="2048x4096 complex int16 speckle pair",
+                shift_px=[3.37, -5.81], noise_frac=0.1, windows=1000, nx=20, ny=50, xsearch=64, ysearch=64,
+                range_interp=2, interp=16, l2="flushed between steps (256 MB write)")
+SPEC = dict(nx=2048, ny=4096, dx=3.37, dy=-5.81, noise_frac=0.1, seed=11)
+
+# algorithmic work per window (5 N log2 N per complex N-point FFT, 6 flops per
+# complex product), split by kernel: range interpolation of both patches and
+# the row halves of the two forward 2-D FFTs run in k_rows; the column halves,
+# the product and the column half of the inverse in k_cols; the row half of
+# the inverse in k_peak; the 8x8 -> 128x128 interpolation in k_subpix.
+def flops_per_window(npx=256, npy=256, ri=2):
+    import math
+    f = lambda n: 5.0 * n * math.log2(n)
+    rng = 2 * npy * (f(npx) + f(ri * npx)) if ri > 1 else 0.0
+    half = npy * f(npx)          # all rows of one 2-D FFT
+    colh = npx * f(npy)          # all columns of one 2-D FFT
+    n2, nx2 = 8, 8 * 16          # 8x8 neighbourhood interpolated by 16: 8 rows then 128 columns
+    sub = (n2 + nx2) * (f(n2) + f(nx2))
+    return {"k_rows": rng + 2 * half, "k_cols": 2 * colh + 6.0 * npx * npy + colh,
+            "k_peak": half, "k_subpix": sub}
+
+
+def algorithmic_bytes_per_window(npx=256, npy=256):
+    return 2 * npx * npy * 4       # both patches as complex int16
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"xcg_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            v = [x.strip() for x in line.split(",")]
+            if len(v) < 9:
+                continue
+            try:
+                sm.append(float(v[1]))
+                smax = float(v[2])
+            except ValueError:
+                continue
+            for n, x in zip(names[1:], v[5:9]):
+                if x.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(m, s, locs, target_s=8.0):
+    """The oracle's FP32 restatement on every host core, repeated over the
+    workload's windows until about target_s seconds have passed."""
+    import xcorr_oracle as xo
+    p = xo.params(64, 64, 2, 1, 16)
+    cores = os.cpu_count() or 1
+    xo.run(p, m, s, locs[:32], precision=xo.F32, nthreads=cores)      # warm (tables, threads)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        xo.run(p, m, s, locs, precision=xo.F32, nthreads=cores, strip_len=20)
+        n += len(locs)
+        dt = time.perf_counter() - t0
+        if dt >= target_s:
+            break
+    return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} windows ({n // len(locs)} passes over the {len(locs)}-window workload) in {dt:.1f} s, "
+                      "oracle FP32 restatement, OpenMP over windows"}
+
+
+def read_traffic():
+    """DRAM bytes per k_rows launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "k_rows_cfg1.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_reference(args):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return
+    from xcorr_gb300 import synth
+    import xcorr_gb300 as xg
+    import xcorr_oracle as xo
+    m, s = synth.make_pair(synth.PairSpec(**SPEC))
+    locs = xg.grid(2048, 4096, 20, 50)
+    p = xo.params(64, 64, 2, 1, 16)
+    cores = os.cpu_count() or 1
+    sample = 64
+    idx = np.linspace(0, len(locs) - 1, sample).astype(int)
+    sl = locs[idx]
+    for _ in range(args.warmup):
+        xo.run(p, m, s, sl, precision=xo.F32, nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        xo.run(p, m, s, sl, precision=xo.F32, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = args.steps * sample / tot
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": dict(WORKLOAD, step_sample=f"{sample} of the 1000 windows per step"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{sample} windows per step, oracle FP32 restatement of the reference path "
+                                       "(the reference has no CPU implementation of this path), OpenMP"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import xcorr_gb300 as xg
+    from xcorr_gb300 import synth
+
+    rank, world, local = _env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    m, s = synth.make_pair(synth.PairSpec(**SPEC))
+    locs = xg.grid(2048, 4096, 20, 50)
+    nwin = len(locs)
+    ctx = xg.Context(xg.params(64, 64, 2, 1, 16), device=dev.index)
+    dm = torch.from_numpy(m).to(dev)
+    ds = torch.from_numpy(s).to(dev)
+    dl = torch.from_numpy(locs).to(dev)
+    dr = torch.zeros((nwin, xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step():
+        ctx.correlate_device(dm.data_ptr(), 2048, 4096, ds.data_ptr(), 2048, 4096, dl.data_ptr(), nwin,
+                             dr.data_ptr(), sp, strip_len=20)
+
+    clocks = ClockSampler(dev.index)
+    clocks.start()                 # sampled through warm-up and the timed steps
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    # device-timed steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches = 0
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+        launches += ctx.stats().launches
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
+    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    dev_ms = float(t.item())
+    value = world * args.steps * nwin / (dev_ms / 1e3)
+
+    # per-kernel times for the roofline (library events on the same stream)
+    ctx.set_profiling(True)
+    kms = [0.0] * 4
+    for _ in range(max(3, min(args.steps, 20))):
+        flush.zero_()
+        step()
+        st = ctx.stats()
+        for k in range(4):
+            kms[k] += st.kernel_ms[k]
+    ctx.set_profiling(False)
+    nprof = max(3, min(args.steps, 20))
+
+    # end to end through the host-buffer entry point, pinned host memory
+    pm = torch.from_numpy(m).pin_memory()
+    ps = torch.from_numpy(s).pin_memory()
+    hostres = np.zeros(nwin, dtype=xg.RESULT_DTYPE)
+    pm_np, ps_np = pm.numpy(), ps.numpy()
+    for _ in range(2):
+        ctx.correlate(pm_np, ps_np, locs, strip_len=20)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hostres = ctx.correlate(pm_np, ps_np, locs, strip_len=20)
+        e2e_t.append(time.perf_counter() - t0)
+    te = torch.tensor([sum(e2e_t)], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = world * args.steps * nwin / float(te.item())
+
+    if rank == 0:
+        import json as _j
+        peaks = {}
+        pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(pk):
+            peaks = _j.load(open(pk))
+        fl = flops_per_window()
+        names = list(xg.KERNEL_NAMES)
+        dom = int(np.argmax(kms))
+        dom_name = names[dom]
+        avg_ms = kms[dom] / nprof
+        ach = fl[dom_name] * nwin / (avg_ms / 1e3) / 1e12
+        smax = peaks.get("sm_max_mhz", 2070.0)
+        fp32_peak = 152 * 128 * 2 * smax * 1e6 / 1e12
+        traffic = read_traffic()
+        hbm_peak = peaks.get("hbm_gbs", 6800.0)
+        roof = {"bound": "fp32_simt", "kernel": dom_name, "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": ach / fp32_peak, "traffic": traffic,
+                "peak_source": "nominal FP32 SIMT rate, 152 SMs x 128 lanes x 2 flop at the measured max SM clock "
+                               f"({smax:.0f} MHz, MEASURED_PEAKS.json); MEASURED_PEAKS.json has no FP32 figure",
+                "algorithmic": f"{fl[dom_name] / 1e6:.2f} MFLOP/window x {nwin} windows per launch",
+                "avg_launch_ms": avg_ms,
+                "hbm": {"achieved": (traffic / (avg_ms / 1e3) / 1e9) if traffic else None, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": ((traffic / (avg_ms / 1e3) / 1e9) / hbm_peak) if traffic else None,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6800"},
+                "kernel_ms_per_step": {n: kms[i] / nprof for i, n in enumerate(names)}}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": WORKLOAD,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(m.nbytes + s.nbytes + locs.nbytes),
+                        "d2h_bytes_per_step": int(hostres.nbytes)},
+                "roofline": roof, "clocks": clk, "gpu_launches": launches,
+                "wall_s_timed": wall}
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(m, s, locs)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

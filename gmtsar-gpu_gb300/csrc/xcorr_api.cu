@@ -100,7 +100,7 @@ struct xcg_ctx {
     void *d_scratch = nullptr;
     size_t scratch_bytes = 0;
     int max_batch = 0;
-    size_t off_zrow, off_amp1, off_amp2c, off_part, off_oob, off_means, off_qspec, off_surf, off_md, off_mdnext, off_corr0n;
+    size_t off_zrow, off_amp1, off_amp2c, off_part, off_oob, off_minmax, off_means, off_qspec, off_surf, off_md, off_mdnext, off_corr0n;
     // host-entry buffers
     void *d_img[2] = {nullptr, nullptr};
     size_t img_bytes[2] = {0, 0};
@@ -149,6 +149,7 @@ static size_t per_window_bytes(const xcg::Plan &B) {
     s += align256((size_t)B.ny_corr * B.nx_corr * sizeof(float));
     s += align256((size_t)2 * B.nchunks * sizeof(float));
     s += align256((size_t)B.nchunks);
+    s += align256((size_t)4 * B.nchunks * sizeof(float));
     s += align256(2 * sizeof(double));
     s += align256((size_t)B.nyc * B.qpitch * sizeof(float2));
     s += align256((size_t)B.nyc * B.nxc * sizeof(float));
@@ -257,6 +258,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         c->off_amp2c = take((size_t)B.ny_corr * B.nx_corr * sizeof(float));
         c->off_part = take((size_t)2 * B.nchunks * sizeof(float));
         c->off_oob = take((size_t)B.nchunks);
+        c->off_minmax = take((size_t)4 * B.nchunks * sizeof(float));
         c->off_means = take(2 * sizeof(double));
         c->off_qspec = take((size_t)B.nyc * B.qpitch * sizeof(float2));
         c->off_surf = take((size_t)B.nyc * B.nxc * sizeof(float));
@@ -326,6 +328,7 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     P.amp2c = (float *)(sc + c->off_amp2c);
     P.part = (float *)(sc + c->off_part);
     P.oobmap = (unsigned char *)(sc + c->off_oob);
+    P.minmax = (float *)(sc + c->off_minmax);
     P.means = (double *)(sc + c->off_means);
     P.qspec = (float2 *)(sc + c->off_qspec);
     P.surf = (float *)(sc + c->off_surf);

@@ -138,6 +138,9 @@ __global__ void __launch_bounds__(128) k_rows(Plan P) {
     const int inx[2] = {P.m_nx, P.s_nx}, iny[2] = {P.m_ny, P.s_ny};
     bool oob = false;
     const int ri = P.ri, lg = P.log2ri;
+    // extremes of the master amplitudes and of the slave amplitudes under the
+    // mask: a patch that is constant and equal to its mean demeans to exact zeros
+    float mn1 = INFINITY, mx1 = -INFINITY, mn2 = INFINITY, mx2 = -INFINITY;
 
     for (int ir = 0; ir < RPC; ir++) {
         const int r = c * RPC + ir;
@@ -194,6 +197,8 @@ __global__ void __launch_bounds__(128) k_rows(Plan P) {
             const float a1 = rb[k], a2 = rb[N + k];
             const bool in = rin && (k >= P.xsearch) && (k < npx - P.xsearch);
             A[fft_pad(k)] = make_float2(a1, in ? a2 : 0.f);
+            mn1 = fminf(mn1, a1); mx1 = fmaxf(mx1, a1);
+            if (in) { mn2 = fminf(mn2, a2); mx2 = fmaxf(mx2, a2); }
             a1g[k] = a1;
             if (r2c && k >= P.xsearch && k < P.xsearch + P.nx_corr) a2g[k - P.xsearch] = a2;
         }
@@ -231,6 +236,17 @@ __global__ void __launch_bounds__(128) k_rows(Plan P) {
         if (lane == 0) P.part[((size_t)w * 2 + pt) * P.nchunks + c] = ac[0];
     }
     if (lane == 0) P.oobmap[(size_t)w * P.nchunks + c] = oob ? 1 : 0;
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) {
+        mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
+        mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
+        mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
+        mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
+    }
+    if (lane == 0) {
+        float *mm = P.minmax + (size_t)w * 4 * P.nchunks;
+        mm[c] = mn1; mm[P.nchunks + c] = mx1; mm[2 * P.nchunks + c] = mn2; mm[3 * P.nchunks + c] = mx2;
+    }
 }
 
 // ---------------------------------------------------------------- k_cols
@@ -373,6 +389,23 @@ __global__ void __launch_bounds__(256) k_peak(Plan P) {
     for (int i = threadIdx.x; i < TWL; i += NT) tw[i] = P.tw_row[i];
     __syncthreads();
 
+    // The reference's surface is exactly zero when either demeaned patch is
+    // (its FFTs of zeros stay zeros); the packed transform here would leave
+    // rounding residue of the other patch, so that case is set explicitly.
+    if (threadIdx.x == 0) {
+        const float *mm = P.minmax + (size_t)w * 4 * P.nchunks;
+        float a = INFINITY, b = -INFINITY, c2 = INFINITY, d = -INFINITY;
+        for (int i = 0; i < P.nchunks; i++) {
+            a = fminf(a, mm[i]); b = fmaxf(b, mm[P.nchunks + i]);
+            c2 = fminf(c2, mm[2 * P.nchunks + i]); d = fmaxf(d, mm[3 * P.nchunks + i]);
+        }
+        const float m1f = (float)P.means[2 * w], m2f = (float)P.means[2 * w + 1];
+        const bool z1 = (a == b) && (a - m1f == 0.f);
+        const bool z2 = (c2 == d) && (c2 - m2f == 0.f);
+        bc[2] = (z1 || z2) ? 0.0 : 1.0;
+    }
+    __syncthreads();
+    const float keep = (float)bc[2];
     unsigned long long best = 0ull;
     double hsum = 0.0, fsum = 0.0;
     const float2 *q = P.qspec + (size_t)w * nyc * P.qpitch;
@@ -389,7 +422,7 @@ __global__ void __launch_bounds__(256) k_peak(Plan P) {
         const float2 *R = team_fft<N, +1>(A, B, tw, lane, T);
         for (int xq = lane; xq < nxc; xq += T) {
             const float2 v = R[fft_pad(xq + P.nx_corr / 2)];
-            const float c1 = fabsf(v.x * scale), c2 = fabsf(v.y * scale);
+            const float c1 = fabsf(v.x * scale) * keep, c2 = fabsf(v.y * scale) * keep;
             surf[(size_t)y1 * nxc + xq] = c1;
             surf[(size_t)y2 * nxc + xq] = c2;
             const unsigned e1 = (unsigned)(y1 * nxc + xq), e2 = (unsigned)(y2 * nxc + xq);

@@ -50,6 +50,7 @@ struct Plan {
     float *amp2c;     // [nwin][ny_corr][nx_corr] slave amplitudes, centre
     float *part;      // [nwin][2][nchunks] FP32 chunk sums (master, slave)
     unsigned char *oobmap;  // [nwin][nchunks] 1 where a chunk read outside its image
+    float *minmax;    // [nwin][4][nchunks] master min/max, masked slave min/max
     double *means;    // [nwin][2]
     float2 *qspec;    // [nwin][nyc][qpitch] column-inverted half spectrum
     float *surf;      // [nwin][nyc][nxc]  correlation surface
