@@ -90,6 +90,11 @@ std::vector<float2> box_spectrum(int n, int lo) {
 
 }  // namespace
 
+namespace xcg {
+// lets other translation units of the library report through xcg_last_error
+void set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+}  // namespace xcg
+
 struct xcg_ctx {
     xcg_params prm;
     int device;

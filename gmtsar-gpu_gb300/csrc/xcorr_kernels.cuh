@@ -10,4 +10,5 @@ void launch_rows(const Plan &P, cudaStream_t s);
 void launch_cols(const Plan &P, cudaStream_t s);
 void launch_peak(const Plan &P, cudaStream_t s);
 void launch_subpix(const Plan &P, cudaStream_t s);
+void set_last_error(const char *msg);
 }  // namespace xcg

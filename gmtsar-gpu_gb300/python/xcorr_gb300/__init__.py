@@ -22,7 +22,9 @@ FLAG_NEXTREAD = 2
 
 # every entry point include/xcorr_gb300.h declares
 EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_create", "xcg_destroy",
-           "xcg_correlate", "xcg_correlate_device", "xcg_set_profiling", "xcg_get_stats")
+           "xcg_correlate", "xcg_correlate_device", "xcg_correlate_device_noalloc", "xcg_set_profiling",
+           "xcg_get_stats")
+NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
 class Params(ctypes.Structure):
@@ -81,6 +83,8 @@ def load(path: str | None = None):
                                 ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]
     L.xcg_correlate_device.restype = ctypes.c_int
     L.xcg_correlate_device.argtypes = L.xcg_correlate.argtypes + [ctypes.c_void_p]
+    L.xcg_correlate_device_noalloc.restype = ctypes.c_int
+    L.xcg_correlate_device_noalloc.argtypes = [ctypes.POINTER(Params)] + L.xcg_correlate.argtypes[1:] + [ctypes.c_void_p]
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
     _lib = L
@@ -154,6 +158,17 @@ class Context:
         _check(self._L.xcg_correlate_device(self._h, d_master, m_nx, m_ny, d_slave, s_nx, s_ny,
                                             int(x_offset), int(y_offset), float(astretcha),
                                             d_locs, nlocs, int(strip_len), d_results, stream))
+
+
+def correlate_device_noalloc(p: Params, d_master: int, m_nx: int, m_ny: int, d_slave: int, s_nx: int, s_ny: int,
+                             d_locs: int, nlocs: int, d_results: int, stream: int = 0, x_offset=0, y_offset=0,
+                             astretcha=0.0, strip_len=0):
+    """xcg_correlate_device_noalloc: device pointers in and out, no context and
+    no device allocation inside the library (scratch is a fixed 32 MiB array)."""
+    L = load()
+    _check(L.xcg_correlate_device_noalloc(ctypes.byref(p), d_master, m_nx, m_ny, d_slave, s_nx, s_ny,
+                                          int(x_offset), int(y_offset), float(astretcha), d_locs, nlocs,
+                                          int(strip_len), d_results, stream))
 
 
 def grid(m_nx, m_ny, nxl, nyl, xsearch=64, ysearch=64):

@@ -118,6 +118,33 @@ xcg_status xcg_correlate_device(xcg_ctx *ctx,
                                 const xcg_loc *d_locs, int32_t nlocs, int32_t strip_len,
                                 xcg_result *d_results, void *stream);
 
+/* Size of the fixed device array behind xcg_correlate_device_noalloc. */
+#define XCG_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* Correlate without allocating any device memory.  No counterpart in the
+ * reference; it exists for callers that must not allocate: code running
+ * inside another framework's device-memory budget (whose caching allocator
+ * owns the free memory, so a cudaMalloc from this library could fail or make
+ * that allocator give back its cache) and code on a latency-critical stream
+ * (cudaMalloc and cudaFree synchronise the device).  The caller passes device
+ * buffers for the images, locations and results, as for
+ * xcg_correlate_device; there is no context.  All scratch, the transform
+ * tables included, comes from one fixed array of XCG_NOALLOC_SCRATCH_BYTES
+ * (32 MiB) that every device loading this library holds until the process
+ * exits: about 30 windows of 128x128 (256x256 FFT) or 120 windows of 64x64
+ * per call.  A call needing more returns XCG_ERR_TOO_LARGE and
+ * xcg_last_error() says how many windows fit.  The first call on each device
+ * looks the array up (set-up work, so make it before any stream capture).
+ * Calls share the array: two calls that overlap on the GPU race and must be
+ * serialised by the caller.  Enqueued on `stream` (a cudaStream_t) of the
+ * current device; returns after enqueueing. */
+xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
+                                        const void *d_master, int32_t m_nx, int32_t m_ny,
+                                        const void *d_slave, int32_t s_nx, int32_t s_ny,
+                                        int32_t x_offset, int32_t y_offset, double astretcha,
+                                        const xcg_loc *d_locs, int32_t nlocs, int32_t strip_len,
+                                        xcg_result *d_results, void *stream);
+
 /* Record CUDA events around every kernel launch (adds a synchronisation at
  * the end of each correlate call to read them). */
 void xcg_set_profiling(xcg_ctx *ctx, int32_t enable);
