@@ -166,3 +166,86 @@ __device__ __forceinline__ float2 *team_fft(float2 *a, float2 *b, const float2 *
 }
 
 }  // namespace xcg
+
+namespace xcg {
+
+// ---------------------------------------------------------------------------
+// Register-resident team FFT.  The same Stockham passes, but the sequence
+// lives in registers between passes: lane l of the team holds elements
+// l + T*m (m < N/T) on entry and the transform's elements l + T*m on exit,
+// and only the passes in between go through shared memory (one padded
+// N-point exchange buffer per team, used in place: every pass reads all its
+// inputs, syncs, then writes).  For N = 256 that is one exchange per FFT.
+// Global loads and stores in the l + T*m layout are coalesced.
+
+__host__ __device__ constexpr int fft_lanes(int n) { return (n / 16 < 32) ? n / 16 : 32; }
+
+template <int N, int DIR, int PASS>
+__device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const float2 *tw, int Ns, int lane) {
+    constexpr int T = fft_lanes(N);
+    constexpr int NP = fft_npasses(N);
+    constexpr int R = fft_radix(N, PASS);
+    constexpr int NR = N / R;
+    constexpr int IT = NR / T;                 // butterflies per lane in this pass
+    static_assert(IT * R * T == N, "team layout");
+    if constexpr (PASS == 0) {
+        // inputs from registers: element (lane + T*it) + NR*r = lane + T*(it + r*IT)
+#pragma unroll
+        for (int it = 0; it < IT; it++) {
+            float2 u[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) u[r] = v[it + r * IT];
+            dft_reg<R, DIR>(u);
+            const int j = lane + T * it;
+#pragma unroll
+            for (int r = 0; r < R; r++) ex[fft_pad(j * R + r)] = u[r];
+        }
+        __syncwarp();
+        team_fft_reg_pass<N, DIR, 1>(v, ex, tw, R, lane);
+    } else if constexpr (PASS < NP) {
+        float2 u[IT][R];
+#pragma unroll
+        for (int it = 0; it < IT; it++) {
+            const int j = lane + T * it;
+            const int k = j & (Ns - 1);
+#pragma unroll
+            for (int r = 0; r < R; r++) u[it][r] = ex[fft_pad(j + r * NR)];
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                const float2 w = tw[(r - 1) * Ns + k];
+                u[it][r] = DIR < 0 ? cmulf(u[it][r], w) : cmulf_conj(u[it][r], w);
+            }
+        }
+        if constexpr (PASS < NP - 1) __syncwarp();
+#pragma unroll
+        for (int it = 0; it < IT; it++) dft_reg<R, DIR>(u[it]);
+        if constexpr (PASS == NP - 1) {
+            // last pass: element j + Ns*r with j = lane + T*it and Ns = NR -> register it + r*IT
+#pragma unroll
+            for (int it = 0; it < IT; it++)
+#pragma unroll
+                for (int r = 0; r < R; r++) v[it + r * IT] = u[it][r];
+            __syncwarp();     // the exchange buffer may be reused right after
+        } else {
+#pragma unroll
+            for (int it = 0; it < IT; it++) {
+                const int j = lane + T * it;
+                const int k = j & (Ns - 1);
+#pragma unroll
+                for (int r = 0; r < R; r++) ex[fft_pad((j - k) * R + k + r * Ns)] = u[it][r];
+            }
+            __syncwarp();
+            team_fft_reg_pass<N, DIR, PASS + 1>(v, ex, tw + (R - 1) * Ns, Ns * R, lane);
+        }
+    }
+}
+
+// In-register N-point FFT of the team's sequence v (N/T values per lane).
+// ex: the team's exchange buffer, fft_padded_len(N) entries.  tw: the
+// size-N pass twiddle table.  All lanes of the warp must call it.
+template <int N, int DIR>
+__device__ __forceinline__ void team_fft_reg(float2 *v, float2 *ex, const float2 *tw, int lane) {
+    team_fft_reg_pass<N, DIR, 0>(v, ex, tw, 1, lane);
+}
+
+}  // namespace xcg

@@ -25,7 +25,6 @@
 
 namespace xcg {
 
-__host__ __device__ constexpr int team_lanes(int n) { return (n / 16 < 32) ? n / 16 : 32; }
 
 // ---------------------------------------------------------------- helpers
 
@@ -101,9 +100,13 @@ __device__ __forceinline__ int slave_row_shift(const Plan &P, int y) {
 // N-point inverse FFT of X[f]*exp(2 pi i f' p / M) / N at q (f' = f or f-N);
 // for p = 0 that is the input sample x[q] itself.  So one forward FFT and
 // ri-1 inverse FFTs of length N give every kept sample.
+//
+// A team of T lanes owns one 1024-sample chunk (1024/N rows) of one window.
+// Rows live in registers in the team layout (lane l: samples l + T*m); the
+// next row's samples are loaded while the current one is transformed.
 template <int N>
-__global__ void __launch_bounds__(128) k_rows(Plan P) {
-    constexpr int T = team_lanes(N);
+__global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_rows(Plan P) {
+    constexpr int T = fft_lanes(N);
     constexpr int TPW = 32 / T;
     constexpr int PADN = fft_padded_len(N);
     constexpr int RPC = (N >= 1024) ? 1 : 1024 / N;     // rows per 1024-sample chunk
@@ -119,11 +122,10 @@ __global__ void __launch_bounds__(128) k_rows(Plan P) {
     const int team = warp * TPW + l32 / T;
     const int teams = blockDim.x / T;
     char *tbase = reinterpret_cast<char *>(tw + TWL) +
-                  (size_t)team * (2 * PADN * sizeof(float2) + 2 * N * sizeof(float) + 2 * ACC * sizeof(float));
-    float2 *A = reinterpret_cast<float2 *>(tbase);
-    float2 *B = A + PADN;
-    float *rb = reinterpret_cast<float *>(B + PADN);    // [2][N]
-    float *acc = rb + 2 * N;                            // [2][ACC]
+                  (size_t)team * (PADN * sizeof(float2) + 2 * N * sizeof(float) + 2 * ACC * sizeof(float));
+    float2 *ex = reinterpret_cast<float2 *>(tbase);
+    float *rb = reinterpret_cast<float *>(ex + PADN);    // [2][N] amplitudes in natural order
+    float *acc = rb + 2 * N;                             // [2][ACC] chunk-sum rows (lane-private slots)
 
     for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_row[i];
     __syncthreads();
@@ -131,109 +133,139 @@ __global__ void __launch_bounds__(128) k_rows(Plan P) {
     const int w = blockIdx.y;
     const int c = blockIdx.x * teams + team;           // chunk (always < nchunks, see launcher)
     const xcg_loc loc = P.locs[w];
-    const int npx = N, npy = P.npy;
-    const int x0[2] = {loc.x - npx / 2, loc.x + P.x_offset - npx / 2};
-    const int y0[2] = {loc.y - npy / 2, loc.y + P.y_offset + slave_row_shift(P, loc.y) - npy / 2};
-    const void *img[2] = {P.master, P.slave};
-    const int inx[2] = {P.m_nx, P.s_nx}, iny[2] = {P.m_ny, P.s_ny};
+    const int npy = P.npy;
+    const int mx0 = loc.x - N / 2, my0 = loc.y - npy / 2;
+    const int sx0 = loc.x + P.x_offset - N / 2;
+    const int sy0 = loc.y + P.y_offset + slave_row_shift(P, loc.y) - npy / 2;
     bool oob = false;
     const int ri = P.ri, lg = P.log2ri;
-    // extremes of the master amplitudes and of the slave amplitudes under the
-    // mask: a patch that is constant and equal to its mean demeans to exact zeros
     float mn1 = INFINITY, mx1 = -INFINITY, mn2 = INFINITY, mx2 = -INFINITY;
 
+    // raw samples of one patch row, team layout; 32-bit words (int16 pair or float)
+    auto load_row = [&](int pt, int r, uint32_t *raw) {
+        const void *img = pt ? P.slave : P.master;
+        const int nx = pt ? P.s_nx : P.m_nx, ny = pt ? P.s_ny : P.m_ny;
+        const int x0 = pt ? sx0 : mx0, y = (pt ? sy0 : my0) + r;
+        const bool rowok = (y >= 0 && y < ny);
+        const uint32_t *row = reinterpret_cast<const uint32_t *>(img) + (size_t)(rowok ? y : 0) * (size_t)nx;
+#pragma unroll
+        for (int m = 0; m < PER; m++) {
+            const int x = x0 + lane + T * m;
+            if (rowok && x >= 0 && x < nx) raw[m] = __ldg(row + x);
+            else { raw[m] = 0u; oob = true; }
+        }
+    };
+    auto to_complex = [&](const uint32_t *raw, float2 *v) {
+#pragma unroll
+        for (int m = 0; m < PER; m++) {
+            if (P.format == 0) {
+                const short lo = (short)(raw[m] & 0xffffu), hi = (short)(raw[m] >> 16);
+                v[m] = make_float2((float)lo, (float)hi);
+            } else {
+                v[m] = make_float2(__uint_as_float(raw[m]), 0.f);
+            }
+        }
+    };
+
+    // amplitudes of one patch row into rb (natural order of the kept fine samples)
+    auto amp_row = [&](int pt, int r, const uint32_t *raw) {
+        float *row = rb + pt * N;
+        float2 v[PER];
+        to_complex(raw, v);
+        if (ri == 1) {
+#pragma unroll
+            for (int m = 0; m < PER; m++) row[lane + T * m] = hypotf(v[m].x, v[m].y);
+            return;
+        }
+        // interpolated rows differ from the reference's cuFFT rows by rounding
+        // anyway, so their amplitudes use the cheaper sqrt(x^2 + y^2); hypotf is
+        // kept where the samples are the input itself (ri == 1, bit-exact)
+#pragma unroll
+        for (int m = 0; m < PER; m++) {          // phase-0 samples are the input
+            const int k = ((lane + T * m) << lg) - N / 2;
+            if (k >= 0 && k < N) row[k] = sqrtf(fmaf(v[m].x, v[m].x, v[m].y * v[m].y));
+        }
+#pragma unroll 1
+        for (int p = 1; p < ri; p++) {
+            if (p > 1) {                             // ri > 2: reread the row (L2) instead of keeping it live
+                uint32_t again[PER];
+                load_row(pt, r, again);
+                to_complex(again, v);
+            }
+            team_fft_reg<N, -1>(v, ex, tw, lane);
+            const float2 *ph = P.phase + (size_t)(p - 1) * N;
+#pragma unroll
+            for (int m = 0; m < PER; m++) v[m] = cmulf(v[m], __ldg(ph + lane + T * m));
+            team_fft_reg<N, +1>(v, ex, tw, lane);
+#pragma unroll
+            for (int m = 0; m < PER; m++) {
+                const int k = ((lane + T * m) << lg) + p - N / 2;
+                if (k >= 0 && k < N) row[k] = sqrtf(fmaf(v[m].x, v[m].x, v[m].y * v[m].y));
+            }
+        }
+    };
+
+    uint32_t rawm[PER], raws[PER];
+    load_row(0, c * RPC, rawm);
+#pragma unroll 1
     for (int ir = 0; ir < RPC; ir++) {
         const int r = c * RPC + ir;
 #pragma unroll 1
         for (int pt = 0; pt < 2; pt++) {
-            float *row = rb + pt * N;
-            for (int k = lane; k < N; k += T)
-                A[fft_pad(k)] = load_sample(P, img[pt], inx[pt], iny[pt], x0[pt] + k, y0[pt] + r, oob);
-            __syncwarp();
-            if (ri == 1) {
-                for (int k = lane; k < N; k += T) {
-                    float2 v = A[fft_pad(k)];
-                    row[k] = hypotf(v.x, v.y);
-                }
-            } else {
-                for (int k = lane; k < N; k += T) {        // phase-0 samples are the input
-                    const int m = N / 2 + k;
-                    if ((m & (ri - 1)) == 0) {
-                        float2 v = A[fft_pad(m >> lg)];
-                        row[k] = hypotf(v.x, v.y);
-                    }
-                }
-                __syncwarp();
-                float2 *S = team_fft<N, -1>(A, B, tw, lane, T);
-                float2 sreg[PER];
+            uint32_t cur[PER];
 #pragma unroll
-                for (int i = 0; i < PER; i++) sreg[i] = S[fft_pad(lane + T * i)];
-                __syncwarp();
-#pragma unroll 1
-                for (int p = 1; p < ri; p++) {
-                    const float2 *ph = P.phase + (size_t)(p - 1) * N;
-#pragma unroll
-                    for (int i = 0; i < PER; i++) A[fft_pad(lane + T * i)] = cmulf(sreg[i], __ldg(ph + lane + T * i));
-                    __syncwarp();
-                    float2 *Y = team_fft<N, +1>(A, B, tw, lane, T);
-                    for (int k = lane; k < N; k += T) {
-                        const int m = N / 2 + k;
-                        if ((m & (ri - 1)) == p) {
-                            float2 v = Y[fft_pad(m >> lg)];
-                            row[k] = hypotf(v.x, v.y);
-                        }
-                    }
-                    __syncwarp();
-                }
-            }
-            __syncwarp();
-        }
-        // packed real pair and its row FFT; amplitudes for the time correlation
-        const bool rin = (r >= P.ysearch) && (r < npy - P.ysearch);
-        float *a1g = P.amp1 + ((size_t)w * npy + r) * npx;
-        const bool r2c = (r >= P.ysearch) && (r < P.ysearch + P.ny_corr);
-        float *a2g = P.amp2c + ((size_t)w * P.ny_corr + (r - P.ysearch)) * P.nx_corr;
-        for (int k = lane; k < N; k += T) {
-            const float a1 = rb[k], a2 = rb[N + k];
-            const bool in = rin && (k >= P.xsearch) && (k < npx - P.xsearch);
-            A[fft_pad(k)] = make_float2(a1, in ? a2 : 0.f);
-            mn1 = fminf(mn1, a1); mx1 = fmaxf(mx1, a1);
-            if (in) { mn2 = fminf(mn2, a2); mx2 = fmaxf(mx2, a2); }
-            a1g[k] = a1;
-            if (r2c && k >= P.xsearch && k < P.xsearch + P.nx_corr) a2g[k - P.xsearch] = a2;
+            for (int m = 0; m < PER; m++) cur[m] = pt ? raws[m] : rawm[m];
+            if (pt == 0) load_row(1, r, raws);                   // in flight during the master row
+            else if (ir + 1 < RPC) load_row(0, r + 1, rawm);     // in flight during the slave row
+            amp_row(pt, r, cur);
         }
         __syncwarp();
-        float2 *Z = team_fft<N, -1>(A, B, tw, lane, T);
-        float2 *zg = P.zrow + ((size_t)w * npy + r) * npx;
-        for (int k = lane; k < N; k += T) zg[k] = Z[fft_pad(k)];
-        // chunk sums in the reference's order: x[t] + x[t+512] first
+        // packed real pair and its row FFT; amplitudes for the time correlation
+        const bool rin = (r >= P.ysearch) && (r < npy - P.ysearch);
+        float *a1g = P.amp1 + ((size_t)w * npy + r) * N;
+        const bool r2c = (r >= P.ysearch) && (r < P.ysearch + P.ny_corr);
+        float *a2g = P.amp2c + ((size_t)w * P.ny_corr + (r - P.ysearch)) * P.nx_corr;
+        float2 v[PER];
 #pragma unroll
-        for (int pt = 0; pt < 2; pt++) {
-            float *ac = acc + pt * ACC;
-            const float *row = rb + pt * N;
-            if (H == 0) {
-                for (int k = lane; k < N; k += T) ac[k] = row[k];
-            } else if (ir < H) {
-                for (int k = lane; k < N; k += T) ac[ir * N + k] = row[k];
-            } else {
-                for (int k = lane; k < N; k += T) ac[(ir - H) * N + k] = ac[(ir - H) * N + k] + row[k];
-            }
+        for (int m = 0; m < PER; m++) {
+            const int e = lane + T * m;
+            const float a1 = rb[e], a2 = rb[N + e];
+            const bool in = rin && (e >= P.xsearch) && (e < N - P.xsearch);
+            v[m] = make_float2(a1, in ? a2 : 0.f);
+            mn1 = fminf(mn1, a1); mx1 = fmaxf(mx1, a1);
+            if (in) { mn2 = fminf(mn2, a2); mx2 = fmaxf(mx2, a2); }
+            a1g[e] = a1;
+            if (r2c && e >= P.xsearch && e < P.xsearch + P.nx_corr) a2g[e - P.xsearch] = a2;
+            // chunk sums in the reference's order: x[t] + x[t+512] first
+            if (H == 0) { acc[e] = a1; acc[ACC + e] = a2; }
+            else if (ir < H) { acc[ir * N + e] = a1; acc[ACC + ir * N + e] = a2; }
+            else { acc[(ir - H) * N + e] = acc[(ir - H) * N + e] + a1; acc[ACC + (ir - H) * N + e] = acc[ACC + (ir - H) * N + e] + a2; }
         }
+        team_fft_reg<N, -1>(v, ex, tw, lane);
+        float2 *zg = P.zrow + ((size_t)w * npy + r) * N;
+#pragma unroll
+        for (int m = 0; m < PER; m++) zg[lane + T * m] = v[m];
         __syncwarp();
     }
     {   // any lane of the team that read outside an image
         const unsigned tmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (l32 - lane));
-        oob = __any_sync(0xffffffffu, oob) && (__ballot_sync(0xffffffffu, oob) & tmask);
+        oob = (__ballot_sync(0xffffffffu, oob) & tmask) != 0u;
     }
-    // remaining tree levels: strides ACC/2 .. 1 (ACC = 1024 only when a chunk is one row)
+    // remaining tree levels, strides ACC/2 .. 1: lane l holds t = l + T*q, so
+    // strides >= T are register-local and smaller ones are team shuffles
 #pragma unroll
     for (int pt = 0; pt < 2; pt++) {
-        float *ac = acc + pt * ACC;
-        for (int st = ACC / 2; st >= 1; st >>= 1) {
-            for (int t = lane; t < st; t += T) ac[t] = ac[t] + ac[t + st];
-            __syncwarp();
-        }
-        if (lane == 0) P.part[((size_t)w * 2 + pt) * P.nchunks + c] = ac[0];
+        float a[ACC / T];
+#pragma unroll
+        for (int q = 0; q < ACC / T; q++) a[q] = acc[pt * ACC + lane + T * q];
+#pragma unroll
+        for (int s = ACC / (2 * T); s >= 1; s >>= 1)
+#pragma unroll
+            for (int q = 0; q < s; q++) a[q] = a[q] + a[q + s];
+        float x = a[0];
+#pragma unroll
+        for (int o = T / 2; o > 0; o >>= 1) x = x + __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) P.part[((size_t)w * 2 + pt) * P.nchunks + c] = x;
     }
     if (lane == 0) P.oobmap[(size_t)w * P.nchunks + c] = oob ? 1 : 0;
 #pragma unroll
@@ -256,21 +288,24 @@ __global__ void __launch_bounds__(128) k_rows(Plan P) {
 // (conv_ampl_demean.cu:713-725) and the demean/mask of d_mean_mask_strip
 // (:111-139), applied here in the frequency domain: the master loses
 // m1*N*M at bin (0,0), the slave m2 times the DFT of its mask.
+// One team per column pair (kx, N-kx); the CTA stages the pairs' columns in
+// shared memory with coalesced row reads and writes the half spectrum back
+// row by row.
 template <int M>
-__global__ void __launch_bounds__(128) k_cols(Plan P) {
-    constexpr int T = team_lanes(M);
+__global__ void __launch_bounds__(128, (M >= 1024) ? 2 : (M >= 512 ? 3 : 4)) k_cols(Plan P) {
+    constexpr int T = fft_lanes(M);
     constexpr int PADM = fft_padded_len(M);
     constexpr int CS = PADM + 1;
-    constexpr int CP = (M <= 256) ? 16 : (M == 512 ? 8 : 4);
+    constexpr int CP = 128 / T;                // column pairs per CTA = teams
     constexpr int TWL = fft_twiddle_len(M);
+    constexpr int PER = M / T;
 
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *cols = tw + TWL;                   // [2*CP][CS]
-    const int teams = blockDim.x / T;
-    float2 *scratch = cols + 2 * CP * CS;      // [teams][PADM]
-    double *sh = reinterpret_cast<double *>(scratch + teams * PADM);   // m1, m2
-    float *pbuf = reinterpret_cast<float *>(sh + 2);                    // [2][nchunks]
+    float2 *exb = cols + 2 * CP * CS;          // [CP][PADM]
+    double *sh = reinterpret_cast<double *>(exb + CP * PADM);   // m1, m2
+    float *pbuf = reinterpret_cast<float *>(sh + 2);             // [2][nchunks]
 
     const int w = blockIdx.y, b = blockIdx.x;
     const int N = P.npx;
@@ -281,12 +316,23 @@ __global__ void __launch_bounds__(128) k_cols(Plan P) {
 
     for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_col[i];
     for (int i = threadIdx.x; i < 2 * P.nchunks; i += blockDim.x) pbuf[i] = P.part[(size_t)w * 2 * P.nchunks + i];
-    for (int i = threadIdx.x; i < 2 * CP * M; i += blockDim.x) {
-        const int s = i % (2 * CP), row = i / (2 * CP);
+    {   // thread t stages slot t % (2CP) for rows t / (2CP) + k * 128/(2CP): all loads first
+        constexpr int RSTEP = 128 / (2 * CP);
+        constexpr int NLD = M / RSTEP;
+        const int s = threadIdx.x % (2 * CP), row0 = threadIdx.x / (2 * CP);
         int col;
         if (s < CP) col = kx0 + s;
         else { const int kx = kx0 + s - CP; col = (kx == 0) ? N / 2 : N - kx; }
-        cols[s * CS + fft_pad(row)] = P.zrow[((size_t)w * M + row) * N + col];
+        const float2 *src = P.zrow + (size_t)w * M * N + col;
+        constexpr int BATCH = (NLD < 16) ? NLD : 16;
+#pragma unroll 1
+        for (int k0 = 0; k0 < NLD; k0 += BATCH) {
+            float2 t[BATCH];
+#pragma unroll
+            for (int k = 0; k < BATCH; k++) t[k] = __ldg(src + (size_t)(row0 + (k0 + k) * RSTEP) * N);
+#pragma unroll
+            for (int k = 0; k < BATCH; k++) cols[s * CS + fft_pad(row0 + (k0 + k) * RSTEP)] = t[k];
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {                      // means in the reference's order (:719-724)
@@ -301,57 +347,64 @@ __global__ void __launch_bounds__(128) k_cols(Plan P) {
     __syncthreads();
     const float dc1 = (float)(sh[0] * (double)N * (double)M);
     const float m2 = (float)sh[1];
-    float2 *scr = scratch + team * PADM;
+    float2 *ex = exb + team * PADM;
 
-    for (int j = team; j < CP; j += teams) {
-        const int kx = kx0 + j;
-        float2 *a = cols + j * CS;
-        float2 *pa = cols + (CP + j) * CS;
-        float2 *ra = team_fft<M, -1>(a, scr, tw, lane, T);
-        if (ra != a) { for (int i = lane; i < M; i += T) a[fft_pad(i)] = ra[fft_pad(i)]; }
-        __syncwarp();
-        float2 *rp = team_fft<M, -1>(pa, scr, tw, lane, T);
-        if (rp != pa) { for (int i = lane; i < M; i += T) pa[fft_pad(i)] = rp[fft_pad(i)]; }
-        __syncwarp();
-        // the kx = 0 team also emits column N/2; the trip count stays warp-uniform
-        // because team_fft ends each pass with a full-warp __syncwarp
-        const int nout = __any_sync(0xffffffffu, kx == 0) ? 2 : 1;
-        for (int o = 0; o < nout; o++) {
-            // o = 0: column kx with partner pa (or itself for kx = 0); o = 1: column N/2, self-paired
-            const float2 *z = (o == 0) ? a : pa;
-            const float2 *zp = (o == 0) ? ((kx == 0) ? a : pa) : pa;
-            const int kxx = (o == 0) ? kx : N / 2;
-            const float2 bx = __ldg(P.box_x + kxx);
-            for (int ky = lane; ky < M; ky += T) {
-                const float2 z1 = z[fft_pad(ky)];
-                const float2 z2 = zp[fft_pad((M - ky) & (M - 1))];
-                // A1 = (z1 + conj z2)/2, A2 = (z1 - conj z2)/(2i)
-                float2 A1 = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-                float2 A2 = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
-                if (kxx == 0 && ky == 0) A1.x -= dc1;
-                const float2 by = __ldg(P.box_y + ky);
-                const float2 bm = cmulf(bx, by);
-                A2.x -= m2 * bm.x;
-                A2.y -= m2 * bm.y;
-                float2 pr = cmulf_conj(A1, A2);
-                if ((kxx + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
-                scr[fft_pad(ky)] = pr;
-            }
-            __syncwarp();
-            float2 *dst = (o == 0) ? a : pa;
-            float2 *rq = team_fft<M, +1>(scr, dst, tw, lane, T);
-            if (rq != dst) { for (int i = lane; i < M; i += T) dst[fft_pad(i)] = rq[fft_pad(i)]; }
-            __syncwarp();
+    const int kx = kx0 + team;
+    float2 *a = cols + team * CS;
+    float2 *pa = cols + (CP + team) * CS;
+    float2 z[PER];
+    // partner column first, back into its slot (read below at -ky)
+#pragma unroll
+    for (int m = 0; m < PER; m++) z[m] = pa[fft_pad(lane + T * m)];
+    team_fft_reg<M, -1>(z, ex, tw, lane);
+#pragma unroll
+    for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
+#pragma unroll
+    for (int m = 0; m < PER; m++) z[m] = a[fft_pad(lane + T * m)];
+    team_fft_reg<M, -1>(z, ex, tw, lane);
+#pragma unroll
+    for (int m = 0; m < PER; m++) a[fft_pad(lane + T * m)] = z[m];
+    __syncwarp();
+    // the kx = 0 team also emits column N/2; the trip count stays warp-uniform
+    // because team_fft_reg synchronises the whole warp
+    const int nout = __any_sync(0xffffffffu, kx == 0) ? 2 : 1;
+#pragma unroll 1
+    for (int o = 0; o < nout; o++) {
+        // o = 0: column kx with partner pa (itself for kx = 0); o = 1: column N/2, self-paired
+        const float2 *zs = (o == 0) ? a : pa;
+        const float2 *zp = (o == 0) ? ((kx == 0) ? a : pa) : pa;
+        const int kxx = (o == 0) ? kx : N / 2;
+        const float2 bx = __ldg(P.box_x + kxx);
+#pragma unroll
+        for (int m = 0; m < PER; m++) {
+            const int ky = lane + T * m;
+            const float2 z1 = zs[fft_pad(ky)];
+            const float2 z2 = zp[fft_pad((M - ky) & (M - 1))];
+            // A1 = (z1 + conj z2)/2, A2 = (z1 - conj z2)/(2i)
+            float2 A1 = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+            float2 A2 = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+            if (kxx == 0 && ky == 0) A1.x -= dc1;
+            const float2 bm = cmulf(bx, __ldg(P.box_y + ky));
+            A2.x -= m2 * bm.x;
+            A2.y -= m2 * bm.y;
+            float2 pr = cmulf_conj(A1, A2);
+            if ((kxx + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
+            z[m] = pr;
         }
+        team_fft_reg<M, +1>(z, ex, tw, lane);
+        float2 *dst = (o == 0) ? a : pa;
+        __syncwarp();
+#pragma unroll
+        for (int m = 0; m < PER; m++) dst[fft_pad(lane + T * m)] = z[m];
+        __syncwarp();
     }
     __syncthreads();
     // write rows y in [ysearch, ysearch+nyc) of the half spectrum, kx <= N/2
     const int nslots = CP + (b == 0 ? 1 : 0);
     for (int i = threadIdx.x; i < nslots * P.nyc; i += blockDim.x) {
         const int s = i % nslots, yq = i / nslots;
-        const int kx = (s < CP) ? kx0 + s : N / 2;
-        const float2 v = cols[s * CS + fft_pad(yq + P.ysearch)];
-        P.qspec[((size_t)w * P.nyc + yq) * P.qpitch + kx] = v;
+        const int kxo = (s < CP) ? kx0 + s : N / 2;
+        P.qspec[((size_t)w * P.nyc + yq) * P.qpitch + kxo] = cols[s * CS + fft_pad(yq + P.ysearch)];
     }
 }
 
@@ -363,16 +416,17 @@ __global__ void __launch_bounds__(128) k_cols(Plan P) {
 // d_scaled_strip (conv_ampl_demean.cu:50-68) and d_cppow_strip (:75-95).
 template <int N>
 __global__ void __launch_bounds__(256) k_peak(Plan P) {
-    constexpr int T = team_lanes(N);
+    constexpr int T = fft_lanes(N);
     constexpr int PADN = fft_padded_len(N);
     constexpr int TWL = fft_twiddle_len(N);
+    constexpr int PER = N / T;
     constexpr int NT = 256;
 
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     const int teams = NT / T;
-    float2 *fb = tw + TWL;                                // [teams][2][PADN]
-    unsigned long long *rk = reinterpret_cast<unsigned long long *>(fb + teams * 2 * PADN);  // [8]
+    float2 *fb = tw + TWL;                                // [teams][PADN]
+    unsigned long long *rk = reinterpret_cast<unsigned long long *>(fb + teams * PADN);  // [8]
     double *rd = reinterpret_cast<double *>(rk + 8);      // [2][8]
     long long *ri64 = reinterpret_cast<long long *>(rd + 16);   // [3][8]
     double *bc = reinterpret_cast<double *>(ri64 + 24);   // broadcast
@@ -381,14 +435,11 @@ __global__ void __launch_bounds__(256) k_peak(Plan P) {
     const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
     const int lane = l32 % T;
     const int team = warp * (32 / T) + l32 / T;
-    float2 *A = fb + team * 2 * PADN;
-    float2 *B = A + PADN;
+    float2 *ex = fb + team * PADN;
     const int M = P.npy, nxc = P.nxc, nyc = P.nyc;
     const float scale = 1.0f / ((float)N * (float)M);
 
     for (int i = threadIdx.x; i < TWL; i += NT) tw[i] = P.tw_row[i];
-    __syncthreads();
-
     // The reference's surface is exactly zero when either demeaned patch is
     // (its FFTs of zeros stay zeros); the packed transform here would leave
     // rounding residue of the other patch, so that case is set explicitly.
@@ -412,28 +463,32 @@ __global__ void __launch_bounds__(256) k_peak(Plan P) {
     float *surf = P.surf + (size_t)w * nyc * nxc;
     for (int pr = team; pr < nyc / 2; pr += teams) {
         const int y1 = 2 * pr, y2 = y1 + 1;
-        for (int kx = lane; kx <= N / 2; kx += T) {
+        // two real rows in one complex inverse FFT: S = Q1 + i Q2, Hermitian-extended
+        float2 v[PER];
+#pragma unroll
+        for (int m = 0; m < PER; m++) {
+            const int e = lane + T * m;
+            const int kx = (e <= N / 2) ? e : N - e;
             float2 q1 = q[(size_t)y1 * P.qpitch + kx], q2 = q[(size_t)y2 * P.qpitch + kx];
             if (kx == 0 || kx == N / 2) { q1.y = 0.f; q2.y = 0.f; }
-            A[fft_pad(kx)] = make_float2(q1.x - q2.y, q1.y + q2.x);
-            if (kx > 0 && kx < N / 2) A[fft_pad(N - kx)] = make_float2(q1.x + q2.y, q2.x - q1.y);
+            v[m] = (e <= N / 2) ? make_float2(q1.x - q2.y, q1.y + q2.x) : make_float2(q1.x + q2.y, q2.x - q1.y);
         }
-        __syncwarp();
-        const float2 *R = team_fft<N, +1>(A, B, tw, lane, T);
-        for (int xq = lane; xq < nxc; xq += T) {
-            const float2 v = R[fft_pad(xq + P.nx_corr / 2)];
-            const float c1 = fabsf(v.x * scale) * keep, c2 = fabsf(v.y * scale) * keep;
+        team_fft_reg<N, +1>(v, ex, tw, lane);
+#pragma unroll
+        for (int m = 0; m < PER; m++) {
+            const int xq = lane + T * m - P.nx_corr / 2;
+            if (xq < 0 || xq >= nxc) continue;
+            const float c1 = fabsf(v[m].x * scale) * keep, c2 = fabsf(v[m].y * scale) * keep;
             surf[(size_t)y1 * nxc + xq] = c1;
             surf[(size_t)y2 * nxc + xq] = c2;
             const unsigned e1 = (unsigned)(y1 * nxc + xq), e2 = (unsigned)(y2 * nxc + xq);
-            unsigned long long k1 = argmax_key(c1, e1), k2 = argmax_key(c2, e2);
+            const unsigned long long k1 = argmax_key(c1, e1), k2 = argmax_key(c2, e2);
             best = k1 > best ? k1 : best;
             best = k2 > best ? k2 : best;
             fsum += (double)c1 + (double)c2;
             if (!(e1 & 512u)) hsum += (double)c1;      // reduce6<double,1024> keeps local [0,512) and [1024,1536)
             if (!(e2 & 512u)) hsum += (double)c2;
         }
-        __syncwarp();
     }
     best = warp_max_u64(best);
     hsum = warp_sum_f64(hsum);
@@ -601,25 +656,24 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
 
 template <int N>
 static size_t rows_smem() {
-    constexpr int T = team_lanes(N);
+    constexpr int T = fft_lanes(N);
     constexpr int ACC = (N >= 1024) ? 1024 : 512;
     const int teams = 128 / T;
     return fft_twiddle_len(N) * sizeof(float2) +
-           (size_t)teams * (2 * fft_padded_len(N) * sizeof(float2) + 2 * N * sizeof(float) + 2 * ACC * sizeof(float));
+           (size_t)teams * (fft_padded_len(N) * sizeof(float2) + 2 * N * sizeof(float) + 2 * ACC * sizeof(float));
 }
 template <int M>
 static size_t cols_smem(int nchunks) {
-    constexpr int T = team_lanes(M);
-    constexpr int CP = (M <= 256) ? 16 : (M == 512 ? 8 : 4);
-    const int teams = 128 / T;
+    constexpr int T = fft_lanes(M);
+    constexpr int CP = 128 / T;
     return fft_twiddle_len(M) * sizeof(float2) + (size_t)2 * CP * (fft_padded_len(M) + 1) * sizeof(float2) +
-           (size_t)teams * fft_padded_len(M) * sizeof(float2) + 2 * sizeof(double) + 2 * nchunks * sizeof(float);
+           (size_t)CP * fft_padded_len(M) * sizeof(float2) + 2 * sizeof(double) + 2 * nchunks * sizeof(float);
 }
 template <int N>
 static size_t peak_smem() {
-    constexpr int T = team_lanes(N);
+    constexpr int T = fft_lanes(N);
     const int teams = 256 / T;
-    return fft_twiddle_len(N) * sizeof(float2) + (size_t)teams * 2 * fft_padded_len(N) * sizeof(float2) +
+    return fft_twiddle_len(N) * sizeof(float2) + (size_t)teams * fft_padded_len(N) * sizeof(float2) +
            8 * sizeof(unsigned long long) + 16 * sizeof(double) + 24 * sizeof(long long) + 4 * sizeof(double);
 }
 static size_t subpix_smem(const Plan &P) {
@@ -663,13 +717,13 @@ cudaError_t kernels_setup(const Plan &P) {
 
 template <int N>
 static void launch_rows_t(const Plan &P, cudaStream_t s) {
-    const int teams = 128 / team_lanes(N);
+    const int teams = 128 / fft_lanes(N);
     dim3 grid(P.nchunks / teams, P.nwin);
     k_rows<N><<<grid, 128, rows_smem<N>(), s>>>(P);
 }
 template <int M>
 static void launch_cols_t(const Plan &P, cudaStream_t s) {
-    constexpr int CP = (M <= 256) ? 16 : (M == 512 ? 8 : 4);
+    constexpr int CP = 128 / fft_lanes(M);
     dim3 grid((P.npx / 2) / CP, P.nwin);
     k_cols<M><<<grid, 128, cols_smem<M>(P.nchunks), s>>>(P);
 }

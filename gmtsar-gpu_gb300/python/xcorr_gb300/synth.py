@@ -128,3 +128,58 @@ def write_case(dirname: str, spec: PairSpec, rshift: int = 0, ashift: int = 0,
     write_prm(os.path.join(dirname, "aligned.PRM"), "aligned.SLC", s.shape[1], s.shape[0], rshift, ashift,
               prf_slave if prf_slave is not None else prf_master)
     return m, s
+
+
+def make_pair_varying(nx: int, ny: int, shift_fn, noise_frac: float, sigma: float = 1000.0, seed: int = 2,
+                      tile: int = 512, margin: int = 64, device=None):
+    """Speckle pair with a spatially varying shift, generated with torch.
+
+    shift_fn(x, y) -> (dx, dy) in pixels, evaluated at the centre of each
+    tile x tile block; each block of the slave is the master delayed by that
+    block's shift (Fourier phase ramp over the block plus `margin` pixels on
+    every side, wrapped at the image border), so the truth is piecewise
+    constant: ``truth(x, y)`` returns the shift of the block holding (x, y).
+    Noise: complex Gaussian at `noise_frac` of the signal power.  Returns
+    (master, slave, truth) with int16 arrays of shape (ny, nx, 2) (numpy);
+    device: a torch device for the transforms (default: cuda if available)."""
+    import torch
+    if device is None:
+        device = torch.device("cuda" if torch.cuda.is_available() else "cpu")
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    m = torch.randn((ny, nx, 2), generator=g, dtype=torch.float32).mul_(sigma).round_().clamp_(-32768, 32767)
+    master = m.to(torch.int16)
+    mz = torch.complex(m[..., 0], m[..., 1]).to(device)
+    out = torch.empty((ny, nx), dtype=torch.complex64, device=device)
+    P = tile + 2 * margin
+    k = torch.fft.fftfreq(P, device=device, dtype=torch.float64)
+    for y0 in range(0, ny, tile):
+        for x0 in range(0, nx, tile):
+            th, tw_ = min(tile, ny - y0), min(tile, nx - x0)
+            dx, dy = shift_fn(x0 + tw_ / 2.0, y0 + th / 2.0)
+            ys = (torch.arange(y0 - margin, y0 - margin + P, device=device) % ny)
+            xs = (torch.arange(x0 - margin, x0 - margin + P, device=device) % nx)
+            blk = mz[ys][:, xs].to(torch.complex128)
+            B = torch.fft.fft2(blk)
+            ramp = torch.exp(-2j * torch.pi * (k[:, None] * dy + k[None, :] * dx))
+            sb = torch.fft.ifft2(B * ramp)
+            out[y0:y0 + th, x0:x0 + tw_] = sb[margin:margin + th, margin:margin + tw_].to(torch.complex64)
+    nz = torch.randn((ny, nx, 2), generator=g, dtype=torch.float32).mul_(sigma * float(np.sqrt(noise_frac)))
+    nz = nz.to(device)
+    sr = (out.real + nz[..., 0]).round_().clamp_(-32768, 32767)
+    si = (out.imag + nz[..., 1]).round_().clamp_(-32768, 32767)
+    slave = torch.stack([sr, si], dim=-1).to(torch.int16).cpu()
+
+    def truth(x, y):
+        bx = (np.asarray(x) // tile) * tile
+        by = (np.asarray(y) // tile) * tile
+        cx = bx + np.minimum(tile, nx - bx) / 2.0
+        cy = by + np.minimum(tile, ny - by) / 2.0
+        return shift_fn(cx, cy)
+
+    return master.numpy(), slave.numpy(), truth
+
+
+def cfg2_shift(x, y):
+    """The full-frame configuration's shift field (px): dx = 2.1 + 1e-5 x - 3e-6 y,
+    dy = -4.7 + 2e-6 x + 8e-6 y."""
+    return 2.1 + 1e-5 * np.asarray(x) - 3e-6 * np.asarray(y), -4.7 + 2e-6 * np.asarray(x) + 8e-6 * np.asarray(y)
