@@ -26,7 +26,7 @@ CLI = os.path.join(BIN_DIR, "xcorr")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC]
-CU_SOURCES = ["xcorr_kernels.cu", "xcorr_api.cu", "xcorr_noalloc.cu"]
+CU_SOURCES = ["xcorr_kernels.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "xcorr_stack.cu"]
 
 
 def _run(cmd):

@@ -18,6 +18,7 @@
 #include "team_fft.cuh"
 #include "xcorr_gb300.h"
 #include "xcorr_kernels.cuh"
+#include "xcorr_ctx.cuh"
 
 using cd = std::complex<double>;
 
@@ -95,29 +96,7 @@ namespace xcg {
 void set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
 }  // namespace xcg
 
-struct xcg_ctx {
-    xcg_params prm;
-    int device;
-    xcg::Plan base;           // sizes and tables; per-batch fields filled at launch
-    // tables
-    float2 *d_tables = nullptr;
-    // scratch
-    void *d_scratch = nullptr;
-    size_t scratch_bytes = 0;
-    int max_batch = 0;
-    size_t off_zrow, off_amp1, off_amp2c, off_part, off_oob, off_minmax, off_means, off_qspec, off_surf, off_md, off_mdnext, off_corr0n;
-    // host-entry buffers
-    void *d_img[2] = {nullptr, nullptr};
-    size_t img_bytes[2] = {0, 0};
-    xcg_loc *d_locs = nullptr;
-    xcg_result *d_res = nullptr;
-    int io_cap = 0;
-    cudaStream_t stream = nullptr;
-    // profiling
-    int profiling = 0;
-    std::vector<cudaEvent_t> events;
-    xcg_stats stats;
-};
+
 
 extern "C" {
 
@@ -314,19 +293,33 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     if (!c || nlocs < 0 || (nlocs > 0 && (!d_master || !d_slave || !d_locs || !d_results))) return XCG_ERR_ARG;
     if (m_nx <= 0 || m_ny <= 0 || s_nx <= 0 || s_ny <= 0 || strip_len < 0) return XCG_ERR_ARG;
     XCG_CK(cudaSetDevice(c->device), "cudaSetDevice");
-    cudaStream_t s = (cudaStream_t)stream;
     memset(&c->stats, 0, sizeof c->stats);
     c->stats.scratch_bytes = c->scratch_bytes;
     if (nlocs == 0) return XCG_OK;
-
     int bw = c->max_batch;
     if (strip_len > 0 && strip_len <= bw) bw = (bw / strip_len) * strip_len;   // keep strips inside a batch
-    xcg::Plan P = c->base;
-    P.master = d_master; P.m_nx = m_nx; P.m_ny = m_ny;
-    P.slave = d_slave; P.s_nx = s_nx; P.s_ny = s_ny;
-    P.x_offset = x_offset; P.y_offset = y_offset; P.astretcha = astretcha;
-    P.strip_len = strip_len;
-    P.nlocs_total = nlocs;
+    xcg::Plan P = xcg::ctx_plan(c);
+    P.single.master = d_master; P.single.m_nx = m_nx; P.single.m_ny = m_ny;
+    P.single.slave = d_slave; P.single.s_nx = s_nx; P.single.s_ny = s_ny;
+    P.single.x_offset = x_offset; P.single.y_offset = y_offset; P.single.astretcha = astretcha;
+    P.single.strip_len = strip_len;
+    P.single.nlocs = nlocs;
+    P.single.out = d_results;
+    P.pairs = nullptr;
+    P.winref = nullptr;
+    P.locs = d_locs;
+    std::vector<int> starts;
+    for (int w = 0; w < nlocs; w += bw) starts.push_back(w);
+    starts.push_back(nlocs);
+    return xcg::ctx_launch(c, P, starts.data(), (int)starts.size() - 1, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+namespace xcg {
+
+Plan ctx_plan(const xcg_ctx *c) {
+    Plan P = c->base;
     char *sc = (char *)c->d_scratch;
     P.zrow = (float2 *)(sc + c->off_zrow);
     P.amp1 = (float *)(sc + c->off_amp1);
@@ -340,8 +333,10 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     P.md = (float *)(sc + c->off_md);
     P.mdnext = (unsigned char *)(sc + c->off_mdnext);
     P.corr0n = (double *)(sc + c->off_corr0n);
+    return P;
+}
 
-    const int nb = (nlocs + bw - 1) / bw;
+xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s) {
     const int nk = P.interp_flag ? 4 : 3;
     if (c->profiling) {
         const size_t need = (size_t)nb * nk * 2;
@@ -351,19 +346,23 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
             c->events.push_back(ev);
         }
     }
-    int ei = 0;
+    const xcg_loc *locs0 = P.locs;
+    const int2 *ref0 = P.winref;
+    int ei = 0, maxw = 0;
     for (int b = 0; b < nb; b++) {
-        P.win0 = b * bw;
-        P.nwin = (nlocs - P.win0 < bw) ? nlocs - P.win0 : bw;
-        P.locs = d_locs + P.win0;
-        P.out = d_results + P.win0;
+        P.win0 = starts[b];
+        P.nwin = starts[b + 1] - starts[b];
+        if (P.nwin > c->max_batch) { set_last_error("batch larger than the context's scratch"); return XCG_ERR_TOO_LARGE; }
+        if (P.nwin > maxw) maxw = P.nwin;
+        P.locs = locs0 + P.win0;
+        P.winref = ref0 ? ref0 + P.win0 : nullptr;
         for (int k = 0; k < nk; k++) {
             if (c->profiling) cudaEventRecord(c->events[ei++], s);
             switch (k) {
-                case 0: xcg::launch_rows(P, s); break;
-                case 1: xcg::launch_cols(P, s); break;
-                case 2: xcg::launch_peak(P, s); break;
-                case 3: xcg::launch_subpix(P, s); break;
+                case 0: launch_rows(P, s); break;
+                case 1: launch_cols(P, s); break;
+                case 2: launch_peak(P, s); break;
+                case 3: launch_subpix(P, s); break;
             }
             if (c->profiling) cudaEventRecord(c->events[ei++], s);
             c->stats.launches++;
@@ -371,8 +370,8 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
-    c->stats.batches = nb;
-    c->stats.batch_windows = bw;
+    c->stats.batches += nb;
+    c->stats.batch_windows = maxw;
     if (c->profiling) {
         XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
         ei = 0;
@@ -386,6 +385,10 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     }
     return XCG_OK;
 }
+
+}  // namespace xcg
+
+extern "C" {
 
 xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m_ny,
                          const void *slave, int32_t s_nx, int32_t s_ny,

@@ -84,8 +84,8 @@ __device__ __forceinline__ float2 load_sample(const Plan &P, const void *img, in
     return make_float2(__ldg(reinterpret_cast<const float *>(img) + i), 0.f);
 }
 
-__device__ __forceinline__ int slave_row_shift(const Plan &P, int y) {
-    return (int)((double)y * P.astretcha);    // ishft, read_xcorr_data.c:65
+__device__ __forceinline__ int slave_row_shift(const PairDev &pd, int y) {
+    return (int)((double)y * pd.astretcha);    // ishft, read_xcorr_data.c:65
 }
 
 // ---------------------------------------------------------------- k_rows
@@ -133,18 +133,23 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     const int w = blockIdx.y;
     const int c = blockIdx.x * teams + team;           // chunk (always < nchunks, see launcher)
     const xcg_loc loc = P.locs[w];
+    int local, pidx;
+    const PairDev pd = pair_of(P, w, local, pidx);
     const int npy = P.npy;
     const int mx0 = loc.x - N / 2, my0 = loc.y - npy / 2;
-    const int sx0 = loc.x + P.x_offset - N / 2;
-    const int sy0 = loc.y + P.y_offset + slave_row_shift(P, loc.y) - npy / 2;
+    const int sx0 = loc.x + pd.x_offset - N / 2;
+    const int sy0 = loc.y + pd.y_offset + slave_row_shift(pd, loc.y) - npy / 2;
     bool oob = false;
     const int ri = P.ri, lg = P.log2ri;
     float mn1 = INFINITY, mx1 = -INFINITY, mn2 = INFINITY, mx2 = -INFINITY;
 
     // raw samples of one patch row, team layout; 32-bit words (int16 pair or float)
     auto load_row = [&](int pt, int r, uint32_t *raw) {
-        const void *img = pt ? P.slave : P.master;
-        const int nx = pt ? P.s_nx : P.m_nx, ny = pt ? P.s_ny : P.m_ny;
+        // image fields re-read per row (parameter space or L1) instead of held in registers
+        const PairDev *q = P.pairs ? P.pairs + pidx : nullptr;
+        const void *img = q ? (pt ? q->slave : q->master) : (pt ? P.single.slave : P.single.master);
+        const int nx = q ? (pt ? q->s_nx : q->m_nx) : (pt ? P.single.s_nx : P.single.m_nx);
+        const int ny = q ? (pt ? q->s_ny : q->m_ny) : (pt ? P.single.s_ny : P.single.m_ny);
         const int x0 = pt ? sx0 : mx0, y = (pt ? sy0 : my0) + r;
         const bool rowok = (y >= 0 && y < ny);
         const uint32_t *row = reinterpret_cast<const uint32_t *>(img) + (size_t)(rowok ? y : 0) * (size_t)nx;
@@ -535,7 +540,9 @@ __global__ void __launch_bounds__(256) k_peak(Plan P) {
         bc[1] = msc;
         const double c0n = (double)surf[0] / msc;
         P.corr0n[w] = c0n;
-        xcg_result &o = P.out[w];
+        int local, pidx;
+        const PairDev pd = pair_of(P, w, local, pidx);
+        xcg_result &o = pd.out[local];
         o.xoff = -1 * jpeak;
         o.yoff = -1 * ipeak;
         o.corr = (float)gamma;
@@ -596,8 +603,15 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
     for (int t = threadIdx.x; t < n2; t += blockDim.x) {
         float v = P.md[(size_t)w * n2 + t];
         if (P.mdnext[(size_t)w * n2 + t]) {
-            const int g = P.win0 + w + 1;    // the reference reads the next window of its strip
-            const bool same = P.strip_len > 0 && g < P.nlocs_total && (g % P.strip_len) != 0 && (w + 1) < P.nwin;
+            // the reference reads the next window of its strip (conv_ampl_demean.cu:84-89)
+            int local, pidx, nlocal = -1, npidx = -1;
+            const PairDev pd = pair_of(P, w, local, pidx);
+            if (w + 1 < P.nwin) {
+                (void)pair_of(P, w + 1, nlocal, npidx);
+                if (npidx != pidx) nlocal = -1;
+            }
+            const int g = local + 1;
+            const bool same = pd.strip_len > 0 && g < pd.nlocs && (g % pd.strip_len) != 0 && nlocal == g;
             v = same ? powf((float)P.corr0n[w + 1], 0.25f) : 0.f;
             atomicOr(fl, XCG_FLAG_NEXTREAD);
         }
@@ -640,7 +654,9 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
         for (int i = 1; i < (int)(blockDim.x >> 5); i++) bb = rk[i] > bb ? rk[i] : bb;
         const unsigned pk = argmax_index(bb);
         const int fip = (int)(pk / (unsigned)nx2), fjp = (int)(pk % (unsigned)nx2);
-        xcg_result &o = P.out[w];
+        int local, pidx;
+        const PairDev pd = pair_of(P, w, local, pidx);
+        xcg_result &o = pd.out[local];
         o.fip = fip;
         o.fjp = fjp;
         o.fmax = argmax_value(bb);
@@ -686,8 +702,10 @@ static cudaError_t setup_rows() {
     return cudaFuncSetAttribute(k_rows<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>());
 }
 template <int M>
-static cudaError_t setup_cols(int nchunks) {
-    return cudaFuncSetAttribute(k_cols<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<M>(nchunks));
+static cudaError_t setup_cols(int) {
+    // the attribute is per kernel, shared by every context: size it for the
+    // largest chunk count any patch width gives (npx <= 1024: nchunks <= M)
+    return cudaFuncSetAttribute(k_cols<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<M>(M));
 }
 template <int N>
 static cudaError_t setup_peak() {
@@ -712,7 +730,10 @@ cudaError_t kernels_setup(const Plan &P) {
         default: return cudaErrorInvalidValue;
     }
     if (e) return e;
-    return cudaFuncSetAttribute(k_subpix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)subpix_smem(P));
+    Plan big = P;                      // the largest interpolated grid any context uses (factor 64)
+    big.nx2 = big.n2x * 64;
+    big.ny2 = big.n2y * 64;
+    return cudaFuncSetAttribute(k_subpix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)subpix_smem(big));
 }
 
 template <int N>

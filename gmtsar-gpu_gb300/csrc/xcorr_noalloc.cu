@@ -222,12 +222,15 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
     P.mdnext = (unsigned char *)(base + s_mdnext);
     P.corr0n = (double *)(base + s_corr0n);
 
-    P.master = d_master; P.m_nx = m_nx; P.m_ny = m_ny;
-    P.slave = d_slave; P.s_nx = s_nx; P.s_ny = s_ny;
-    P.x_offset = x_offset; P.y_offset = y_offset; P.astretcha = astretcha;
-    P.locs = d_locs; P.nwin = nlocs; P.win0 = 0; P.nlocs_total = nlocs;
-    P.strip_len = strip_len;
-    P.out = d_results;
+    P.single.master = d_master; P.single.m_nx = m_nx; P.single.m_ny = m_ny;
+    P.single.slave = d_slave; P.single.s_nx = s_nx; P.single.s_ny = s_ny;
+    P.single.x_offset = x_offset; P.single.y_offset = y_offset; P.single.astretcha = astretcha;
+    P.single.strip_len = strip_len;
+    P.single.nlocs = nlocs;
+    P.single.out = d_results;
+    P.pairs = nullptr;
+    P.winref = nullptr;
+    P.locs = d_locs; P.nwin = nlocs; P.win0 = 0;
 
     e = xcg::kernels_setup(P);
     if (e != cudaSuccess) { snprintf(t_msg, sizeof t_msg, "kernel attributes: %s", cudaGetErrorString(e)); return fail_msg(XCG_ERR_CUDA); }

@@ -7,6 +7,20 @@
 
 namespace xcg {
 
+// One image pair as the kernels see it: device images, PRM offsets, the
+// pair's result array and strip length.
+struct PairDev {
+    const void *master;
+    int m_nx, m_ny;
+    const void *slave;
+    int s_nx, s_ny;
+    int x_offset, y_offset;
+    double astretcha;
+    xcg_result *out;       // results of this pair, indexed by the window's index within the pair
+    int nlocs;             // windows of this pair
+    int strip_len;         // 0: no cross-window read
+};
+
 struct Plan {
     // geometry (parse_xcorr_input.c:67-86)
     int npx, npy;          // patch: 4*xsearch x 4*ysearch
@@ -19,21 +33,15 @@ struct Plan {
     int nchunks;           // 1024-sample chunks per patch (npx*npy/1024)
     int qpitch;            // row pitch (complex) of the half-spectrum rows: npx/2 + 16
 
-    // images
-    const void *master;
-    int m_nx, m_ny;
-    const void *slave;
-    int s_nx, s_ny;
-    int x_offset, y_offset;
-    double astretcha;
+    // image pairs: one pair by value, or a table with a per-window reference
+    PairDev single;        // used when pairs == nullptr
+    const PairDev *pairs;  // stack of pairs (device)
+    const int2 *winref;    // [nwin] (pair, index within the pair), offset to the batch
 
     // windows of this batch
     const xcg_loc *locs;   // already offset to the batch's first window
     int nwin;              // windows in this batch
-    int strip_len;         // 0: no cross-window read
-    int win0;              // global index of the batch's first window
-    int nlocs_total;
-    xcg_result *out;       // offset to the batch's first window
+    int win0;              // single pair: index of the batch's first window
 
     // tables (device, built on the host in double)
     const float2 *tw_row;   // Stockham twiddles for npx
@@ -58,5 +66,20 @@ struct Plan {
     unsigned char *mdnext;  // [nwin][n2y*n2x] 1 where the next window's value goes
     double *corr0n;   // [nwin]
 };
+
+// The pair of batch window w (a copy: taking the address of the kernel
+// parameter would force the whole plan into local memory), the window's index
+// within that pair and the pair's index in the table.
+__device__ __forceinline__ PairDev pair_of(const Plan &P, int w, int &local, int &pidx) {
+    if (P.pairs) {
+        const int2 r = P.winref[w];
+        local = r.y;
+        pidx = r.x;
+        return P.pairs[r.x];
+    }
+    local = P.win0 + w;
+    pidx = 0;
+    return P.single;
+}
 
 }  // namespace xcg

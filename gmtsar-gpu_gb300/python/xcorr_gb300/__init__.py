@@ -23,7 +23,8 @@ FLAG_NEXTREAD = 2
 # every entry point include/xcorr_gb300.h declares
 EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_create", "xcg_destroy",
            "xcg_correlate", "xcg_correlate_device", "xcg_correlate_device_noalloc", "xcg_set_profiling",
-           "xcg_get_stats")
+           "xcg_get_stats", "xcg_stack_create", "xcg_stack_destroy", "xcg_stack_run", "xcg_stack_set_graph",
+           "xcg_stack_autotune", "xcg_stack_get_stats")
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
@@ -52,6 +53,23 @@ class Stats(ctypes.Structure):
 
 
 KERNEL_NAMES = ("k_rows", "k_cols", "k_peak", "k_subpix")
+
+
+class Pair(ctypes.Structure):
+    """xcg_pair: one pair of a stack (device images and results, host locations)."""
+    _fields_ = [("d_master", ctypes.c_void_p), ("m_nx", ctypes.c_int32), ("m_ny", ctypes.c_int32),
+                ("d_slave", ctypes.c_void_p), ("s_nx", ctypes.c_int32), ("s_ny", ctypes.c_int32),
+                ("x_offset", ctypes.c_int32), ("y_offset", ctypes.c_int32), ("astretcha", ctypes.c_double),
+                ("locs", ctypes.c_void_p), ("nlocs", ctypes.c_int32), ("strip_len", ctypes.c_int32),
+                ("xsearch", ctypes.c_int32), ("ysearch", ctypes.c_int32), ("d_results", ctypes.c_void_p)]
+
+
+class StackStats(ctypes.Structure):
+    _fields_ = [("windows", ctypes.c_int64), ("launches", ctypes.c_int64), ("graph_replays", ctypes.c_int64),
+                ("last_graph_launches", ctypes.c_int64), ("batches", ctypes.c_int32),
+                ("last_graph_batches", ctypes.c_int32), ("buckets", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("bucket_npx", ctypes.c_int32 * 8), ("bucket_npy", ctypes.c_int32 * 8),
+                ("bucket_batch", ctypes.c_int32 * 8)]
 
 _lib = None
 
@@ -85,6 +103,15 @@ def load(path: str | None = None):
     L.xcg_correlate_device.argtypes = L.xcg_correlate.argtypes + [ctypes.c_void_p]
     L.xcg_correlate_device_noalloc.restype = ctypes.c_int
     L.xcg_correlate_device_noalloc.argtypes = [ctypes.POINTER(Params)] + L.xcg_correlate.argtypes[1:] + [ctypes.c_void_p]
+    L.xcg_stack_create.restype = ctypes.c_int
+    L.xcg_stack_create.argtypes = [ctypes.POINTER(Params), ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
+    L.xcg_stack_destroy.argtypes = [ctypes.c_void_p]
+    L.xcg_stack_run.restype = ctypes.c_int
+    L.xcg_stack_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(Pair), ctypes.c_int32, ctypes.c_void_p]
+    L.xcg_stack_autotune.restype = ctypes.c_int
+    L.xcg_stack_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Pair), ctypes.c_int32, ctypes.c_void_p]
+    L.xcg_stack_set_graph.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    L.xcg_stack_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(StackStats)]
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
     _lib = L
@@ -158,6 +185,51 @@ class Context:
         _check(self._L.xcg_correlate_device(self._h, d_master, m_nx, m_ny, d_slave, s_nx, s_ny,
                                             int(x_offset), int(y_offset), float(astretcha),
                                             d_locs, nlocs, int(strip_len), d_results, stream))
+
+
+class Stack:
+    """A stack of pairs correlated together (xcg_stack_*).  common: ri,
+    interpolation and format shared by every pair."""
+
+    def __init__(self, common: Params, device: int = 0):
+        self._L = load()
+        h = ctypes.c_void_p()
+        _check(self._L.xcg_stack_create(ctypes.byref(common), device, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._L.xcg_stack_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _array(pairs):
+        arr = (Pair * len(pairs))()
+        for i, p in enumerate(pairs):
+            arr[i] = p
+        return arr
+
+    def run(self, pairs, stream: int = 0):
+        arr = self._array(pairs)
+        _check(self._L.xcg_stack_run(self._h, arr, len(pairs), stream))
+
+    def autotune(self, pairs, stream: int = 0):
+        arr = self._array(pairs)
+        _check(self._L.xcg_stack_autotune(self._h, arr, len(pairs), stream))
+
+    def set_graph(self, on: bool):
+        self._L.xcg_stack_set_graph(self._h, 1 if on else 0)
+
+    def stats(self) -> StackStats:
+        s = StackStats()
+        self._L.xcg_stack_get_stats(self._h, ctypes.byref(s))
+        return s
 
 
 def correlate_device_noalloc(p: Params, d_master: int, m_nx: int, m_ny: int, d_slave: int, s_nx: int, s_ny: int,

@@ -145,6 +145,48 @@ xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
                                         const xcg_loc *d_locs, int32_t nlocs, int32_t strip_len,
                                         xcg_result *d_results, void *stream);
 
+/* ---- Stack scheduler ----
+ * A stack of interferogram pairs correlated in one pass: windows are
+ * bucketed by geometry (xsearch x ysearch, i.e. FFT size), each bucket runs
+ * in batches of whole strips, and the whole stack can be captured into one
+ * CUDA graph and replayed.  No counterpart in the reference, which runs one
+ * pair per xcorr process (xcorr.cu:437-490). */
+typedef struct {
+    const void *d_master;  int32_t m_nx, m_ny;   /* DEVICE image, format as the stack's params */
+    const void *d_slave;   int32_t s_nx, s_ny;
+    int32_t x_offset, y_offset;                  /* rshift, ashift */
+    double astretcha;
+    const xcg_loc *locs;                         /* HOST array of nlocs locations */
+    int32_t nlocs, strip_len;
+    int32_t xsearch, ysearch;                    /* this pair's window geometry */
+    xcg_result *d_results;                       /* DEVICE array of nlocs results */
+} xcg_pair;
+
+typedef struct {
+    int64_t windows, launches, graph_replays, last_graph_launches;
+    int32_t batches, last_graph_batches, buckets, pad;
+    int32_t bucket_npx[8], bucket_npy[8], bucket_batch[8];
+} xcg_stack_stats;
+
+typedef struct xcg_stack xcg_stack;
+
+/* common: ri, interp_flag, interp_factor, n2x/n2y, format of every pair
+ * (its xsearch/ysearch are ignored: each pair carries its own). */
+xcg_status xcg_stack_create(const xcg_params *common, int32_t device, xcg_stack **out);
+void xcg_stack_destroy(xcg_stack *st);
+/* Correlate every window of every pair; enqueued on `stream`.  The location
+ * arrays are read before return; images and result arrays are used
+ * asynchronously. */
+xcg_status xcg_stack_run(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, void *stream);
+/* Graph mode: a run captures the stack's uploads and launches into a CUDA
+ * graph on `stream` (not the legacy stream); later runs with identical pairs
+ * and locations replay it. */
+void xcg_stack_set_graph(xcg_stack *st, int32_t enable);
+/* Time candidate batch sizes per bucket on these pairs and keep the fastest
+ * (appended to the file named by XCG_TUNE_CACHE, read back by new buckets). */
+xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, void *stream);
+void xcg_stack_get_stats(const xcg_stack *st, xcg_stack_stats *out);
+
 /* Record CUDA events around every kernel launch (adds a synchronisation at
  * the end of each correlate call to read them). */
 void xcg_set_profiling(xcg_ctx *ctx, int32_t enable);
