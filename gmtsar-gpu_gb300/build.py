@@ -26,7 +26,14 @@ CLI = os.path.join(BIN_DIR, "xcorr")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC]
-CU_SOURCES = ["xcorr_kernels.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "xcorr_stack.cu"]
+def _cuda_home():
+    import shutil
+    nv = shutil.which(NVCC) or NVCC
+    home = os.environ.get("CUDA_HOME") or os.path.dirname(os.path.dirname(os.path.realpath(nv)))
+    return home
+
+
+CU_SOURCES = ["xcorr_kernels.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "xcorr_stack.cu", "refiner.cu", "refiner_api.cu"]
 
 
 def _run(cmd):
@@ -71,8 +78,12 @@ def build_cli(force=False):
         return None
     deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")] + [LIB]
     if force or _stale(CLI, deps):
-        _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-I" + INC, "-I" + HOST] + srcs +
-             ["-L" + LIB_DIR, "-lxcorr_gb300", "-Wl,-rpath,$ORIGIN/../lib", "-lm", "-o", CLI])
+        cuda = _cuda_home()
+        culib = next((d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib"))
+                      if os.path.isdir(d)), os.path.join(cuda, "lib64"))
+        _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-I" + INC, "-I" + HOST, "-I" + os.path.join(cuda, "include")] +
+             srcs + ["-L" + LIB_DIR, "-lxcorr_gb300", "-Wl,-rpath,$ORIGIN/../lib", "-L" + culib, "-lcudart",
+                     "-Wl,-rpath," + culib, "-lpthread", "-lm", "-o", CLI])
     return CLI
 
 

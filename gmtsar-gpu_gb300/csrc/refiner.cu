@@ -1,0 +1,484 @@
+// Subpixel refiner: a small CNN that reads the normalised 9x9 correlation
+// surface around the integer peak and predicts the subpixel peak position
+// (fx, fy, in surface pixels, the quantities highres_corr returns as
+// xfrac/yfrac, highres_corr.cu:67-76) and the log variance s of that
+// estimate.  No counterpart in the reference; it stands in for the FFT
+// zero-pad interpolation where it is confident.
+//
+// Network (valid 3x3 convolutions, GELU): 9x9 -> 32@7x7 -> 32@5x5 -> 32@3x3
+// -> dense 64 -> dense 3.  37,507 parameters, FP32 master copy.
+//   training:  k_ref_fwd (FP32, keeps activations) -> k_ref_bwd (activation
+//              gradients per sample) -> k_ref_wgrad (parameter gradients,
+//              fixed-order reductions over the batch) -> k_ref_adam
+//   inference: k_ref_infer, BF16 weights and activations on the tensor cores
+//              (mma.sync m16n8k16, FP32 accumulation), conv+GELU fused with
+//              the activations in shared memory.
+// Loss per sample: 0.5 r^2 + 0.5 stopgrad(r^2) exp(-s) + s.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "refiner.cuh"
+
+namespace xcg {
+
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_g(float x) {
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+// ---------------------------------------------------------------- training forward
+// One warp per sample, lane = channel.  Activations (pre- and post-GELU) go to
+// the per-sample record `act` for the backward pass.
+__global__ void __launch_bounds__(128) k_ref_fwd(RefPlan R, const float *__restrict__ feat, int n) {
+    extern __shared__ float sm[];
+    float *W2t = sm;                 // [288][32]: (k*9+d, c)
+    float *W3t = W2t + 9216;
+    const int warp = threadIdx.x >> 5, c = threadIdx.x & 31;
+    float *ws = W3t + 9216 + warp * 2816;
+    float *x0 = ws, *a1 = x0 + 96, *a2 = a1 + 1568, *a3 = a2 + 800, *g1 = a3 + 288;
+    for (int i = threadIdx.x; i < 9216; i += blockDim.x) { W2t[i] = R.w2t[i]; W3t[i] = R.w3t[i]; }
+    __syncthreads();
+    const float *P = R.theta;
+    for (int s = blockIdx.x * 4 + warp; s < n; s += gridDim.x * 4) {
+        float *act = R.act + (size_t)s * REF_ACT;
+        for (int i = c; i < 81; i += 32) x0[i] = feat[(size_t)s * 81 + i];
+        __syncwarp();
+        for (int p = 0; p < 49; p++) {
+            const int i = p / 7, j = p % 7;
+            float y = P[RP_B1 + c];
+#pragma unroll
+            for (int d = 0; d < 9; d++) y = fmaf(P[RP_W1 + c * 9 + d], x0[(i + d / 3) * 9 + j + d % 3], y);
+            act[ACT_Y1 + c * 49 + p] = y;
+            const float a = gelu_f(y);
+            a1[c * 49 + p] = a;
+            act[ACT_A1 + c * 49 + p] = a;
+        }
+        __syncwarp();
+        for (int p = 0; p < 25; p++) {
+            const int i = p / 5, j = p % 5;
+            float y = P[RP_B2 + c];
+            for (int k = 0; k < 32; k++)
+#pragma unroll
+                for (int d = 0; d < 9; d++) y = fmaf(W2t[(k * 9 + d) * 32 + c], a1[k * 49 + (i + d / 3) * 7 + j + d % 3], y);
+            act[ACT_Y2 + c * 25 + p] = y;
+            const float a = gelu_f(y);
+            a2[c * 25 + p] = a;
+            act[ACT_A2 + c * 25 + p] = a;
+        }
+        __syncwarp();
+        for (int p = 0; p < 9; p++) {
+            const int i = p / 3, j = p % 3;
+            float y = P[RP_B3 + c];
+            for (int k = 0; k < 32; k++)
+#pragma unroll
+                for (int d = 0; d < 9; d++) y = fmaf(W3t[(k * 9 + d) * 32 + c], a2[k * 25 + (i + d / 3) * 5 + j + d % 3], y);
+            act[ACT_Y3 + c * 9 + p] = y;
+            const float a = gelu_f(y);
+            a3[c * 9 + p] = a;
+            act[ACT_A3 + c * 9 + p] = a;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int h2 = 0; h2 < 2; h2++) {
+            const int o = c + 32 * h2;
+            float z = P[RP_C1 + o];
+            for (int h = 0; h < 288; h++) z = fmaf(R.f1t[h * 64 + o], a3[h], z);
+            act[ACT_Z1 + o] = z;
+            const float g = gelu_f(z);
+            g1[o] = g;
+            act[ACT_G1 + o] = g;
+        }
+        __syncwarp();
+        if (c < 3) {
+            float o = P[RP_C2 + c];
+            for (int k = 0; k < 64; k++) o = fmaf(P[RP_F2 + c * 64 + k], g1[k], o);
+            act[ACT_OUT + c] = o;
+            if (R.out) R.out[(size_t)s * 3 + c] = o;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- training backward
+// One warp per sample: gradients of the loss w.r.t. every pre-activation.
+__global__ void __launch_bounds__(128) k_ref_bwd(RefPlan R, const float *__restrict__ target, int n) {
+    extern __shared__ float sm[];
+    float *W2 = sm;                  // parameter layout [c][k][3][3]
+    float *W3 = W2 + 9216;
+    const int warp = threadIdx.x >> 5, c = threadIdx.x & 31;
+    float *ws = W3 + 9216 + warp * 1184;
+    float *dout = ws, *dz1 = dout + 4, *dy3 = dz1 + 64, *dy2 = dy3 + 288;
+    for (int i = threadIdx.x; i < 9216; i += blockDim.x) { W2[i] = R.theta[RP_W2 + i]; W3[i] = R.theta[RP_W3 + i]; }
+    __syncthreads();
+    const float *P = R.theta;
+    const float inv_n = 1.0f / (float)n;
+    for (int s = blockIdx.x * 4 + warp; s < n; s += gridDim.x * 4) {
+        const float *act = R.act + (size_t)s * REF_ACT;
+        float *gr = R.grad_act + (size_t)s * REF_ACT;
+        if (c == 0) {
+            const float fx = act[ACT_OUT], fy = act[ACT_OUT + 1], lv = act[ACT_OUT + 2];
+            const float rx = fx - target[2 * s], ry = fy - target[2 * s + 1];
+            const float r2 = rx * rx + ry * ry;
+            dout[0] = rx * inv_n;
+            dout[1] = ry * inv_n;
+            dout[2] = (1.0f - 0.5f * r2 * expf(-lv)) * inv_n;
+            if (R.loss) R.loss[s] = 0.5f * r2 + 0.5f * r2 * expf(-lv) + lv;
+            gr[ACT_OUT] = dout[0]; gr[ACT_OUT + 1] = dout[1]; gr[ACT_OUT + 2] = dout[2];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int h2 = 0; h2 < 2; h2++) {
+            const int k = c + 32 * h2;
+            float g = 0.f;
+#pragma unroll
+            for (int o = 0; o < 3; o++) g = fmaf(P[RP_F2 + o * 64 + k], dout[o], g);
+            const float dz = g * gelu_g(act[ACT_Z1 + k]);
+            dz1[k] = dz;
+            gr[ACT_Z1 + k] = dz;
+        }
+        __syncwarp();
+        for (int q = 0; q < 9; q++) {
+            const int h = c * 9 + q;
+            float g = 0.f;
+            for (int o = 0; o < 64; o++) g = fmaf(P[RP_F1 + o * 288 + h], dz1[o], g);
+            const float dy = g * gelu_g(act[ACT_Y3 + h]);
+            dy3[h] = dy;
+            gr[ACT_Y3 + h] = dy;
+        }
+        __syncwarp();
+        // conv3 input gradient: lane k, positions of the 5x5 input
+        for (int p = 0; p < 25; p++) {
+            const int pi = p / 5, pj = p % 5;
+            float g = 0.f;
+            for (int co = 0; co < 32; co++)
+#pragma unroll
+                for (int d = 0; d < 9; d++) {
+                    const int oi = pi - d / 3, oj = pj - d % 3;
+                    if (oi >= 0 && oi < 3 && oj >= 0 && oj < 3) g = fmaf(W3[co * 288 + c * 9 + d], dy3[co * 9 + oi * 3 + oj], g);
+                }
+            const float dy = g * gelu_g(act[ACT_Y2 + c * 25 + p]);
+            dy2[c * 25 + p] = dy;
+            gr[ACT_Y2 + c * 25 + p] = dy;
+        }
+        __syncwarp();
+        for (int p = 0; p < 49; p++) {
+            const int pi = p / 7, pj = p % 7;
+            float g = 0.f;
+            for (int co = 0; co < 32; co++)
+#pragma unroll
+                for (int d = 0; d < 9; d++) {
+                    const int oi = pi - d / 3, oj = pj - d % 3;
+                    if (oi >= 0 && oi < 5 && oj >= 0 && oj < 5) g = fmaf(W2[co * 288 + c * 9 + d], dy2[co * 25 + oi * 5 + oj], g);
+                }
+            gr[ACT_Y1 + c * 49 + p] = g * gelu_g(act[ACT_Y1 + c * 49 + p]);
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------- parameter gradients
+// Fixed-order reductions over the batch (no atomics, reproducible).
+// Blocks: [0,1024) W2 (c,k); [1024,2048) W3 (c,k); [2048,2080) W1 + biases of
+// channel c; [2080,2144) F1 row o + c1[o]; 2144: F2 + c2.
+__device__ __forceinline__ float block_sum(float v, float *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[w] = v;
+    __syncthreads();
+    float t = 0.f;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += red[i];
+    return t;
+}
+
+__global__ void __launch_bounds__(128) k_ref_wgrad(RefPlan R, const float *__restrict__ feat, int n) {
+    __shared__ float red[8];
+    const int b = blockIdx.x;
+    const float *A = R.act, *G = R.grad_act;
+    float *g = R.grad;
+    if (b < 2048) {
+        const bool l3 = b >= 1024;
+        const int cc = (b & 1023) >> 5, k = b & 31;
+        const int Ho = l3 ? 3 : 5, Hi = l3 ? 5 : 7;
+        const int oG = l3 ? ACT_Y3 : ACT_Y2, oA = l3 ? ACT_A2 : ACT_A1;
+        float acc[9];
+#pragma unroll
+        for (int d = 0; d < 9; d++) acc[d] = 0.f;
+        for (int s = threadIdx.x; s < n; s += blockDim.x) {
+            const float *dy = G + (size_t)s * REF_ACT + oG + cc * Ho * Ho;
+            const float *a = A + (size_t)s * REF_ACT + oA + k * Hi * Hi;
+            for (int p = 0; p < Ho * Ho; p++) {
+                const float v = dy[p];
+                const int i = p / Ho, j = p % Ho;
+#pragma unroll
+                for (int d = 0; d < 9; d++) acc[d] = fmaf(v, a[(i + d / 3) * Hi + j + d % 3], acc[d]);
+            }
+        }
+        for (int d = 0; d < 9; d++) {
+            const float t = block_sum(acc[d], red);
+            if (threadIdx.x == 0) g[(l3 ? RP_W3 : RP_W2) + cc * 288 + k * 9 + d] = t;
+        }
+    } else if (b < 2080) {
+        const int cc = b - 2048;
+        float acc[9], sb1 = 0.f, sb2 = 0.f, sb3 = 0.f;
+#pragma unroll
+        for (int d = 0; d < 9; d++) acc[d] = 0.f;
+        for (int s = threadIdx.x; s < n; s += blockDim.x) {
+            const float *dy = G + (size_t)s * REF_ACT + ACT_Y1 + cc * 49;
+            const float *x = feat + (size_t)s * 81;
+            for (int p = 0; p < 49; p++) {
+                const float v = dy[p];
+                sb1 += v;
+                const int i = p / 7, j = p % 7;
+#pragma unroll
+                for (int d = 0; d < 9; d++) acc[d] = fmaf(v, x[(i + d / 3) * 9 + j + d % 3], acc[d]);
+            }
+            for (int p = 0; p < 25; p++) sb2 += G[(size_t)s * REF_ACT + ACT_Y2 + cc * 25 + p];
+            for (int p = 0; p < 9; p++) sb3 += G[(size_t)s * REF_ACT + ACT_Y3 + cc * 9 + p];
+        }
+        for (int d = 0; d < 9; d++) {
+            const float t = block_sum(acc[d], red);
+            if (threadIdx.x == 0) g[RP_W1 + cc * 9 + d] = t;
+        }
+        float t = block_sum(sb1, red); if (threadIdx.x == 0) g[RP_B1 + cc] = t;
+        t = block_sum(sb2, red); if (threadIdx.x == 0) g[RP_B2 + cc] = t;
+        t = block_sum(sb3, red); if (threadIdx.x == 0) g[RP_B3 + cc] = t;
+    } else if (b < 2144) {
+        const int o = b - 2080;
+        // thread h accumulates F1[o][h] over the batch (h = tid, tid+128, tid+256)
+        for (int h = threadIdx.x; h < 288; h += blockDim.x) {
+            float acc = 0.f;
+            for (int s = 0; s < n; s++) acc = fmaf(G[(size_t)s * REF_ACT + ACT_Z1 + o], A[(size_t)s * REF_ACT + ACT_A3 + h], acc);
+            g[RP_F1 + o * 288 + h] = acc;
+        }
+        float sb = 0.f;
+        for (int s = threadIdx.x; s < n; s += blockDim.x) sb += G[(size_t)s * REF_ACT + ACT_Z1 + o];
+        const float t = block_sum(sb, red);
+        if (threadIdx.x == 0) g[RP_C1 + o] = t;
+    } else {
+        for (int e = threadIdx.x; e < 192 + 3; e += blockDim.x) {
+            float acc = 0.f;
+            if (e < 192) {
+                const int o = e / 64, k = e % 64;
+                for (int s = 0; s < n; s++) acc = fmaf(G[(size_t)s * REF_ACT + ACT_OUT + o], A[(size_t)s * REF_ACT + ACT_G1 + k], acc);
+                g[RP_F2 + e] = acc;
+            } else {
+                for (int s = 0; s < n; s++) acc += G[(size_t)s * REF_ACT + ACT_OUT + (e - 192)];
+                g[RP_C2 + e - 192] = acc;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- Adam + derived copies
+__global__ void k_ref_adam(RefPlan R, float lr, float b1, float b2, float eps, float c1, float c2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < RP_N; i += gridDim.x * blockDim.x) {
+        const float gi = R.grad[i];
+        const float m = b1 * R.m[i] + (1.f - b1) * gi;
+        const float v = b2 * R.v[i] + (1.f - b2) * gi * gi;
+        R.m[i] = m;
+        R.v[i] = v;
+        R.theta[i] = R.theta[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
+    }
+}
+
+// transposed FP32 copies for the training forward and BF16 copies for inference
+__global__ void k_ref_derive(RefPlan R) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < RP_N; i += gridDim.x * blockDim.x) {
+        const float t = R.theta[i];
+        R.wbf[i] = __float2bfloat16_rn(t);
+        if (i >= RP_W2 && i < RP_W2 + 9216) { const int e = i - RP_W2, c = e / 288, kk = e % 288; R.w2t[kk * 32 + c] = t; }
+        if (i >= RP_W3 && i < RP_W3 + 9216) { const int e = i - RP_W3, c = e / 288, kk = e % 288; R.w3t[kk * 32 + c] = t; }
+        if (i >= RP_F1 && i < RP_F1 + 18432) { const int e = i - RP_F1, o = e / 288, h = e % 288; R.f1t[h * 64 + o] = t; }
+    }
+}
+
+// ---------------------------------------------------------------- inference, BF16 tensor cores
+// mma.sync m16n8k16 row.col bf16 -> f32.  Fragment layout (PTX ISA): with
+// g = lane/4, t = lane%4, A regs {a0: (g, 2t..2t+1), a1: (g+8, 2t..), a2: (g, 2t+8..),
+// a3: (g+8, 2t+8..)}, B regs {b0: (k=2t..2t+1, n=g), b1: (k=2t+8.., n=g)},
+// C {c0,c1: (g, 2t..2t+1), c2,c3: (g+8, 2t..2t+1)}.
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+// One 16-row tile of a GEMM with N = 8*NT columns and K = 288: acc[nt] +=
+// A(16 x 288) * B(288 x 8nt).  fetchA(row, kk) returns the bf16 element (0 for
+// padded rows); Bs is [n][288] bf16 in shared memory.
+template <int NT, class FA>
+__device__ __forceinline__ void tile_gemm_288(float (&acc)[NT][4], FA fetchA, const __nv_bfloat16 *Bs, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll 2
+    for (int ks = 0; ks < 18; ks++) {
+        const int k0 = ks * 16 + 2 * t;
+        uint32_t a[4];
+        a[0] = pack2(fetchA(g, k0), fetchA(g, k0 + 1));
+        a[1] = pack2(fetchA(g + 8, k0), fetchA(g + 8, k0 + 1));
+        a[2] = pack2(fetchA(g, k0 + 8), fetchA(g, k0 + 9));
+        a[3] = pack2(fetchA(g + 8, k0 + 8), fetchA(g + 8, k0 + 9));
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++) {
+            const __nv_bfloat16 *bp = Bs + (size_t)(nt * 8 + g) * 288 + k0;
+            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(bp);
+            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(bp + 8);
+            mma_bf16(acc[nt], a, b0, b1);
+        }
+    }
+}
+
+// Each warp takes 4 windows at a time: conv1 on the SIMT pipes (K = 9), conv2,
+// conv3 and the dense 288 -> 64 layer as tensor-core tiles with bias + GELU
+// applied to the accumulators, the 64 -> 3 layer on SIMT.
+__global__ void __launch_bounds__(128) k_ref_infer(RefPlan R, const float *__restrict__ feat, float *__restrict__ out, int n) {
+    extern __shared__ __align__(16) unsigned char smc[];
+    __nv_bfloat16 *B2 = reinterpret_cast<__nv_bfloat16 *>(smc);    // W2 [32][288]
+    __nv_bfloat16 *B3 = B2 + 9216;                                  // W3 [32][288]
+    __nv_bfloat16 *BF = B3 + 9216;                                  // F1 [64][288]
+    float *small = reinterpret_cast<float *>(BF + 18432);            // W1 (288), b1, b2, b3 (96), c1 (64), F2 (192), c2 (3)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char *wbase = reinterpret_cast<unsigned char *>(small + 648) + warp * WARP_INFER_BYTES;
+    float *x0 = reinterpret_cast<float *>(wbase);                               // [4][81]
+    __nv_bfloat16 *a1 = reinterpret_cast<__nv_bfloat16 *>(x0 + 4 * 84);        // [4][32][49]
+    __nv_bfloat16 *a2 = a1 + 4 * 32 * 49;                                       // [4][32][25]
+    __nv_bfloat16 *a3 = a2 + 4 * 32 * 25;                                       // [4][288]
+    float *g1 = reinterpret_cast<float *>(a3 + 4 * 288);                        // [4][64]
+    for (int i = threadIdx.x; i < 9216; i += blockDim.x) { B2[i] = R.wbf[RP_W2 + i]; B3[i] = R.wbf[RP_W3 + i]; }
+    for (int i = threadIdx.x; i < 18432; i += blockDim.x) BF[i] = R.wbf[RP_F1 + i];
+    for (int i = threadIdx.x; i < 288; i += blockDim.x) small[i] = R.theta[RP_W1 + i];
+    for (int i = threadIdx.x; i < 32; i += blockDim.x) {
+        small[288 + i] = R.theta[RP_B1 + i]; small[320 + i] = R.theta[RP_B2 + i]; small[352 + i] = R.theta[RP_B3 + i];
+    }
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) small[384 + i] = R.theta[RP_C1 + i];
+    for (int i = threadIdx.x; i < 195; i += blockDim.x) small[448 + i] = R.theta[RP_F2 + i];   // F2 then c2
+    __syncthreads();
+    const float *W1 = small, *b1 = small + 288, *b2 = small + 320, *b3 = small + 352, *c1 = small + 384;
+    const float *F2 = small + 448, *c2 = small + 448 + 192;
+    const int g = lane >> 2, t = lane & 3;
+    const int ngroups = (n + 3) / 4;
+    for (int grp = blockIdx.x * 4 + warp; grp < ngroups; grp += gridDim.x * 4) {
+        const int s0 = grp * 4;
+        const int nw = min(4, n - s0);
+        for (int i = lane; i < 4 * 81; i += 32) {
+            const int wl = i / 81, e = i % 81;
+            x0[wl * 84 + e] = (wl < nw) ? feat[(size_t)(s0 + wl) * 81 + e] : 0.f;
+        }
+        __syncwarp();
+        // conv1: lane = channel
+        for (int wl = 0; wl < 4; wl++)
+            for (int p = 0; p < 49; p++) {
+                const int i = p / 7, j = p % 7;
+                float y = b1[lane];
+#pragma unroll
+                for (int d = 0; d < 9; d++) y = fmaf(W1[lane * 9 + d], x0[wl * 84 + (i + d / 3) * 9 + j + d % 3], y);
+                a1[(wl * 32 + lane) * 49 + p] = __float2bfloat16_rn(gelu_f(y));
+            }
+        __syncwarp();
+        // conv2: rows (window, position) = 100 in 7 tiles of 16
+        for (int mt = 0; mt < 7; mt++) {
+            float acc[4][4] = {};
+            auto fa = [&](int r, int kk) -> __nv_bfloat16 {
+                const int m = mt * 16 + r;
+                if (m >= 100) return __float2bfloat16_rn(0.f);
+                const int wl = m / 25, p = m % 25, k = kk / 9, d = kk % 9;
+                return a1[(wl * 32 + k) * 49 + (p / 5 + d / 3) * 7 + p % 5 + d % 3];
+            };
+            tile_gemm_288<4>(acc, fa, B2, lane);
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int m = mt * 16 + g + (h >> 1) * 8, ch = nt * 8 + 2 * t + (h & 1);
+                    if (m < 100) a2[((m / 25) * 32 + ch) * 25 + m % 25] = __float2bfloat16_rn(gelu_f(acc[nt][h] + b2[ch]));
+                }
+        }
+        __syncwarp();
+        // conv3: rows (window, position) = 36 in 3 tiles
+        for (int mt = 0; mt < 3; mt++) {
+            float acc[4][4] = {};
+            auto fa = [&](int r, int kk) -> __nv_bfloat16 {
+                const int m = mt * 16 + r;
+                if (m >= 36) return __float2bfloat16_rn(0.f);
+                const int wl = m / 9, p = m % 9, k = kk / 9, d = kk % 9;
+                return a2[(wl * 32 + k) * 25 + (p / 3 + d / 3) * 5 + p % 3 + d % 3];
+            };
+            tile_gemm_288<4>(acc, fa, B3, lane);
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int m = mt * 16 + g + (h >> 1) * 8, ch = nt * 8 + 2 * t + (h & 1);
+                    if (m < 36) a3[(m / 9) * 288 + ch * 9 + m % 9] = __float2bfloat16_rn(gelu_f(acc[nt][h] + b3[ch]));
+                }
+        }
+        __syncwarp();
+        // dense 288 -> 64: rows = 4 windows (padded to 16)
+        {
+            float acc[8][4] = {};
+            auto fa = [&](int r, int kk) -> __nv_bfloat16 {
+                return (r < 4) ? a3[r * 288 + kk] : __float2bfloat16_rn(0.f);
+            };
+            tile_gemm_288<8>(acc, fa, BF, lane);
+#pragma unroll
+            for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int m = g + (h >> 1) * 8, o = nt * 8 + 2 * t + (h & 1);
+                    if (m < 4) g1[m * 64 + o] = gelu_f(acc[nt][h] + c1[o]);
+                }
+        }
+        __syncwarp();
+        if (lane < 12) {
+            const int wl = lane / 3, o = lane % 3;
+            float v = c2[o];
+            for (int k = 0; k < 64; k++) v = fmaf(F2[o * 64 + k], g1[wl * 64 + k], v);
+            if (wl < nw) out[(size_t)(s0 + wl) * 3 + o] = v;
+        }
+        __syncwarp();
+    }
+}
+
+size_t ref_fwd_smem() { return (size_t)(2 * 9216 + 4 * 2816) * sizeof(float); }
+size_t ref_bwd_smem() { return (size_t)(2 * 9216 + 4 * 1184) * sizeof(float); }
+size_t ref_infer_smem() {
+    return (size_t)(9216 * 2 + 18432) * sizeof(__nv_bfloat16) + 648 * sizeof(float) + 4 * (size_t)WARP_INFER_BYTES;
+}
+
+cudaError_t ref_setup() {
+    cudaError_t e = cudaFuncSetAttribute(k_ref_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ref_fwd_smem());
+    if (!e) e = cudaFuncSetAttribute(k_ref_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ref_bwd_smem());
+    if (!e) e = cudaFuncSetAttribute(k_ref_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ref_infer_smem());
+    return e;
+}
+
+void ref_launch_fwd(const RefPlan &R, const float *feat, int n, cudaStream_t s) {
+    const int blocks = (n + 3) / 4 < 608 ? (n + 3) / 4 : 608;
+    k_ref_fwd<<<blocks, 128, ref_fwd_smem(), s>>>(R, feat, n);
+}
+void ref_launch_bwd(const RefPlan &R, const float *target, int n, cudaStream_t s) {
+    const int blocks = (n + 3) / 4 < 608 ? (n + 3) / 4 : 608;
+    k_ref_bwd<<<blocks, 128, ref_bwd_smem(), s>>>(R, target, n);
+}
+void ref_launch_wgrad(const RefPlan &R, const float *feat, int n, cudaStream_t s) {
+    k_ref_wgrad<<<2145, 128, 0, s>>>(R, feat, n);
+}
+void ref_launch_adam(const RefPlan &R, float lr, int step, cudaStream_t s) {
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    k_ref_adam<<<(RP_N + 255) / 256, 256, 0, s>>>(R, lr, b1, b2, 1e-8f, c1, c2);
+}
+void ref_launch_derive(const RefPlan &R, cudaStream_t s) { k_ref_derive<<<(RP_N + 255) / 256, 256, 0, s>>>(R); }
+void ref_launch_infer(const RefPlan &R, const float *feat, float *out, int n, cudaStream_t s) {
+    const int groups = (n + 3) / 4;
+    const int blocks = (groups + 3) / 4 < 456 ? (groups + 3) / 4 : 456;
+    k_ref_infer<<<blocks > 0 ? blocks : 1, 128, ref_infer_smem(), s>>>(R, feat, out, n);
+}
+
+}  // namespace xcg

@@ -231,8 +231,8 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         XCG_CK_C(cudaMemGetInfo(&freeb, &totb), "cudaMemGetInfo");
         size_t budget = (size_t)8 << 30;
         if (budget > freeb * 2 / 5) budget = freeb * 2 / 5;
-        int mb = max_batch > 0 ? max_batch : 4096;
-        if ((size_t)mb * pw > budget) mb = (int)(budget / pw);
+        int mb = max_batch > 0 ? max_batch : 2048;
+        if ((size_t)mb * pw * c->nslots > budget) mb = (int)(budget / (pw * c->nslots));
         if (mb < 1) { st = XCG_ERR_NOMEM; g_last_error = "not enough device memory for one window"; goto fail; }
         c->max_batch = mb;
         size_t off = 0;
@@ -249,9 +249,15 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         c->off_md = take(64 * sizeof(float));
         c->off_mdnext = take(64);
         c->off_corr0n = take(sizeof(double));
-        c->scratch_bytes = off;
-        XCG_CK_C(cudaMalloc(&c->d_scratch, off), "cudaMalloc scratch");
+        c->slot_bytes = align256(off);
+        c->scratch_bytes = c->slot_bytes * (size_t)c->nslots;
+        XCG_CK_C(cudaMalloc(&c->d_scratch, c->scratch_bytes), "cudaMalloc scratch");
         XCG_CK_C(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (int k = 0; k < c->nslots; k++) {
+            XCG_CK_C(cudaStreamCreateWithFlags(&c->slot_stream[k], cudaStreamNonBlocking), "cudaStreamCreate");
+            XCG_CK_C(cudaEventCreateWithFlags(&c->ev_join[k], cudaEventDisableTiming), "cudaEventCreate");
+        }
+        XCG_CK_C(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
     }
 #undef XCG_CK_C
     c->stats.scratch_bytes = c->scratch_bytes;
@@ -272,9 +278,21 @@ void xcg_destroy(xcg_ctx *c) {
     cudaFree(c->d_img[1]);
     cudaFree(c->d_locs);
     cudaFree(c->d_res);
+    cudaFree(c->ref_feat);
+    cudaFree(c->ref_pred);
+    cudaFree(c->ref_skip);
     for (cudaEvent_t ev : c->events) cudaEventDestroy(ev);
+    for (int k = 0; k < 2; k++) {
+        if (c->slot_stream[k]) { cudaStreamSynchronize(c->slot_stream[k]); cudaStreamDestroy(c->slot_stream[k]); }
+        if (c->ev_join[k]) cudaEventDestroy(c->ev_join[k]);
+    }
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+void xcg_set_features(xcg_ctx *c, float *d_features) {
+    if (c) c->features = d_features;
 }
 
 void xcg_set_profiling(xcg_ctx *c, int32_t enable) {
@@ -297,7 +315,11 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     c->stats.scratch_bytes = c->scratch_bytes;
     if (nlocs == 0) return XCG_OK;
     int bw = c->max_batch;
-    if (strip_len > 0 && strip_len <= bw) bw = (bw / strip_len) * strip_len;   // keep strips inside a batch
+    // enough windows for two batches of >= 256: split so the two slots overlap
+    if (nlocs >= 512 && (nlocs + 1) / 2 < bw) bw = (nlocs + 1) / 2;
+    if (strip_len > 0 && strip_len <= bw) bw = ((bw + strip_len - 1) / strip_len) * strip_len;   // whole strips
+    if (bw > c->max_batch) bw = (c->max_batch / (strip_len > 0 ? strip_len : 1)) * (strip_len > 0 ? strip_len : 1);
+    if (bw < 1) bw = c->max_batch;
     xcg::Plan P = xcg::ctx_plan(c);
     P.single.master = d_master; P.single.m_nx = m_nx; P.single.m_ny = m_ny;
     P.single.slave = d_slave; P.single.s_nx = s_nx; P.single.s_ny = s_ny;
@@ -305,6 +327,7 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     P.single.strip_len = strip_len;
     P.single.nlocs = nlocs;
     P.single.out = d_results;
+    P.single.feat = c->features;
     P.pairs = nullptr;
     P.winref = nullptr;
     P.locs = d_locs;
@@ -336,6 +359,16 @@ Plan ctx_plan(const xcg_ctx *c) {
     return P;
 }
 
+// The plan with every scratch pointer moved by off bytes (another slot).
+static Plan with_slot(Plan P, size_t off) {
+    if (!off) return P;
+    auto mv = [off](auto *p) { return reinterpret_cast<decltype(p)>(reinterpret_cast<char *>(p) + off); };
+    P.zrow = mv(P.zrow); P.amp1 = mv(P.amp1); P.amp2c = mv(P.amp2c); P.part = mv(P.part);
+    P.oobmap = mv(P.oobmap); P.minmax = mv(P.minmax); P.means = mv(P.means); P.qspec = mv(P.qspec);
+    P.surf = mv(P.surf); P.md = mv(P.md); P.mdnext = mv(P.mdnext); P.corr0n = mv(P.corr0n);
+    return P;
+}
+
 xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s) {
     const int nk = P.interp_flag ? 4 : 3;
     if (c->profiling) {
@@ -349,23 +382,40 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     const xcg_loc *locs0 = P.locs;
     const int2 *ref0 = P.winref;
     int ei = 0, maxw = 0;
+    // batches alternate between the scratch slots on the slot streams (forked
+    // from and joined back into s); profiling runs them in order on s so each
+    // kernel's events time that kernel alone
+    const bool fork = nb > 1 && c->nslots > 1 && !c->profiling;
+    if (fork) {
+        XCG_CK(cudaEventRecord(c->ev_fork, s), "cudaEventRecord");
+        for (int k = 0; k < c->nslots; k++) XCG_CK(cudaStreamWaitEvent(c->slot_stream[k], c->ev_fork, 0), "cudaStreamWaitEvent");
+    }
     for (int b = 0; b < nb; b++) {
-        P.win0 = starts[b];
-        P.nwin = starts[b + 1] - starts[b];
-        if (P.nwin > c->max_batch) { set_last_error("batch larger than the context's scratch"); return XCG_ERR_TOO_LARGE; }
-        if (P.nwin > maxw) maxw = P.nwin;
-        P.locs = locs0 + P.win0;
-        P.winref = ref0 ? ref0 + P.win0 : nullptr;
+        const int slot = fork ? b % c->nslots : 0;
+        cudaStream_t ss = fork ? c->slot_stream[slot] : s;
+        Plan Q = with_slot(P, (size_t)slot * c->slot_bytes);
+        Q.win0 = starts[b];
+        Q.nwin = starts[b + 1] - starts[b];
+        if (Q.nwin > c->max_batch) { set_last_error("batch larger than the context's scratch"); return XCG_ERR_TOO_LARGE; }
+        if (Q.nwin > maxw) maxw = Q.nwin;
+        Q.locs = locs0 + Q.win0;
+        Q.winref = ref0 ? ref0 + Q.win0 : nullptr;
         for (int k = 0; k < nk; k++) {
-            if (c->profiling) cudaEventRecord(c->events[ei++], s);
+            if (c->profiling) cudaEventRecord(c->events[ei++], ss);
             switch (k) {
-                case 0: launch_rows(P, s); break;
-                case 1: launch_cols(P, s); break;
-                case 2: launch_peak(P, s); break;
-                case 3: launch_subpix(P, s); break;
+                case 0: launch_rows(Q, ss); break;
+                case 1: launch_cols(Q, ss); break;
+                case 2: launch_peak(Q, ss); break;
+                case 3: launch_subpix(Q, ss); break;
             }
-            if (c->profiling) cudaEventRecord(c->events[ei++], s);
+            if (c->profiling) cudaEventRecord(c->events[ei++], ss);
             c->stats.launches++;
+        }
+    }
+    if (fork) {
+        for (int k = 0; k < c->nslots; k++) {
+            XCG_CK(cudaEventRecord(c->ev_join[k], c->slot_stream[k]), "cudaEventRecord");
+            XCG_CK(cudaStreamWaitEvent(s, c->ev_join[k], 0), "cudaStreamWaitEvent");
         }
     }
     cudaError_t e = cudaGetLastError();

@@ -15,8 +15,14 @@ struct xcg_ctx {
     float2 *d_tables = nullptr;
     // scratch
     void *d_scratch = nullptr;
-    size_t scratch_bytes = 0;
-    int max_batch = 0;
+    size_t scratch_bytes = 0;     // all slots
+    size_t slot_bytes = 0;        // one slot: scratch for max_batch windows
+    int max_batch = 0;            // windows per batch (per slot)
+    // consecutive batches alternate between slots on their own streams, so
+    // one batch's column/peak stages overlap the next batch's row stage
+    int nslots = 2;
+    cudaStream_t slot_stream[2] = {nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
     size_t off_zrow, off_amp1, off_amp2c, off_part, off_oob, off_minmax, off_means, off_qspec, off_surf, off_md,
         off_mdnext, off_corr0n;
     // host-entry buffers
@@ -26,6 +32,12 @@ struct xcg_ctx {
     xcg_result *d_res = nullptr;
     int io_cap = 0;
     cudaStream_t stream = nullptr;
+    // optional per-window 9x9 neighbourhoods written by xcg_correlate_device
+    float *features = nullptr;
+    // buffers of the refined path (xcg_correlate_device_refined)
+    float *ref_feat = nullptr, *ref_pred = nullptr;
+    unsigned char *ref_skip = nullptr;
+    int ref_cap = 0;
     // profiling
     int profiling = 0;
     std::vector<cudaEvent_t> events;

@@ -560,6 +560,19 @@ __global__ void __launch_bounds__(256) k_peak(Plan P) {
         o.fip = -1; o.fjp = -1; o.fmax = 0.f; o.xfrac = 0.f; o.yfrac = 0.f;
     }
     __syncthreads();
+    // normalised 9x9 neighbourhood of the integer peak, for the subpixel refiner
+    {
+        int local, pidx;
+        const PairDev pd = pair_of(P, w, local, pidx);
+        if (pd.feat) {
+            for (int t = threadIdx.x; t < 81; t += NT) {
+                const int yy = ip - 4 + t / 9, xx = jp - 4 + t % 9;
+                float v = 0.f;
+                if (cmax > 0.0 && yy >= 0 && yy < nyc && xx >= 0 && xx < nxc) v = (float)((double)surf[yy * nxc + xx] / cmax);
+                pd.feat[(size_t)local * 81 + t] = v;
+            }
+        }
+    }
     // 8x8 neighbourhood with the reference's flat bounds test (conv_ampl_demean.cu:82-93)
     if (P.interp_flag) {
         const int n2 = P.n2x * P.n2y;
@@ -597,6 +610,7 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
     int *fl = reinterpret_cast<int *>(rk + 8);
 
     const int w = blockIdx.x;
+    if (P.skip && P.skip[w]) return;                  // the refiner answered for this window
     const int n2 = n2x * n2y;
     if (threadIdx.x == 0) *fl = 0;
     __syncthreads();
@@ -666,6 +680,44 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
         o.yfrac = ipeak / (float)P.ifc;
         o.flags |= *fl;
     }
+}
+
+// ---------------------------------------------------------------- k_decide
+// Takes the refiner's (fx, fy, s) for each window of the batch when it is
+// confident: predicted standard deviation exp(s/2) below max_sigma and both
+// coordinates within max_dis of a three-point parabola fit of the 9x9
+// neighbourhood; those windows get xfrac = fx, yfrac = fy (surface pixels,
+// as highres_corr.cu:67-76 defines them) and XCG_FLAG_REFINED, and are
+// skipped by k_subpix.
+__global__ void k_decide(Plan P, const float *__restrict__ pred, unsigned char *skip, float max_sigma, float max_dis) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= P.nwin) return;
+    int local, pidx;
+    const PairDev pd = pair_of(P, w, local, pidx);
+    const float *f = pd.feat + (size_t)local * 81;
+    const float fx = pred[3 * w], fy = pred[3 * w + 1], sg = expf(0.5f * pred[3 * w + 2]);
+    auto vertex = [](float a, float b, float c) {
+        const float den = a - 2.f * b + c;
+        return (den < 0.f) ? 0.5f * (a - c) / den : 0.f;
+    };
+    const float px = vertex(f[4 * 9 + 3], f[4 * 9 + 4], f[4 * 9 + 5]);
+    const float py = vertex(f[3 * 9 + 4], f[4 * 9 + 4], f[5 * 9 + 4]);
+    const bool ok = (sg < max_sigma) && fabsf(fx - px) < max_dis && fabsf(fy - py) < max_dis &&
+                    isfinite(fx) && isfinite(fy) && f[4 * 9 + 4] > 0.f;
+    skip[w] = ok ? 1 : 0;
+    if (ok) {
+        xcg_result &o = pd.out[local];
+        o.xfrac = fx;
+        o.yfrac = fy;
+        o.fip = -1;
+        o.fjp = -1;
+        o.flags |= XCG_FLAG_REFINED;
+    }
+}
+
+void launch_decide(const Plan &P, const float *pred, unsigned char *skip, float max_sigma, float max_dis,
+                   cudaStream_t s) {
+    k_decide<<<(P.nwin + 127) / 128, 128, 0, s>>>(P, pred, skip, max_sigma, max_dis);
 }
 
 // ---------------------------------------------------------------- launchers

@@ -19,6 +19,7 @@ struct PairDev {
     xcg_result *out;       // results of this pair, indexed by the window's index within the pair
     int nlocs;             // windows of this pair
     int strip_len;         // 0: no cross-window read
+    float *feat;           // [nlocs][81] normalised 9x9 neighbourhood of the integer peak, or null
 };
 
 struct Plan {
@@ -65,6 +66,7 @@ struct Plan {
     float *md;        // [nwin][n2y*n2x]  neighbourhood ^0.25, NaN-safe
     unsigned char *mdnext;  // [nwin][n2y*n2x] 1 where the next window's value goes
     double *corr0n;   // [nwin]
+    const unsigned char *skip;  // [nwin] 1: the subpixel stage leaves this window alone (null: none)
 };
 
 // The pair of batch window w (a copy: taking the address of the kernel

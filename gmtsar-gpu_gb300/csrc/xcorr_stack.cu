@@ -157,7 +157,7 @@ static xcg_status plan_run(xcg_stack *st, const xcg_pair *pairs, int npairs) {
         pd.master = q.d_master; pd.m_nx = q.m_nx; pd.m_ny = q.m_ny;
         pd.slave = q.d_slave; pd.s_nx = q.s_nx; pd.s_ny = q.s_ny;
         pd.x_offset = q.x_offset; pd.y_offset = q.y_offset; pd.astretcha = q.astretcha;
-        pd.out = q.d_results; pd.nlocs = q.nlocs; pd.strip_len = q.strip_len;
+        pd.out = q.d_results; pd.nlocs = q.nlocs; pd.strip_len = q.strip_len; pd.feat = q.d_features;
         for (int l = 0; l < q.nlocs; l++) {
             b.h_locs[b.nwin + l] = q.locs[l];
             b.h_ref[b.nwin + l] = make_int2(pi, l);

@@ -24,7 +24,11 @@ FLAG_NEXTREAD = 2
 EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_create", "xcg_destroy",
            "xcg_correlate", "xcg_correlate_device", "xcg_correlate_device_noalloc", "xcg_set_profiling",
            "xcg_get_stats", "xcg_stack_create", "xcg_stack_destroy", "xcg_stack_run", "xcg_stack_set_graph",
-           "xcg_stack_autotune", "xcg_stack_get_stats")
+           "xcg_stack_autotune", "xcg_stack_get_stats", "xcg_set_features", "xcg_refiner_create",
+           "xcg_refiner_destroy", "xcg_refiner_set_params", "xcg_refiner_get_params", "xcg_refiner_forward",
+           "xcg_refiner_gradient", "xcg_refiner_train_step", "xcg_correlate_device_refined")
+REFINER_NPARAM = 37507
+FLAG_REFINED = 4
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
@@ -61,7 +65,8 @@ class Pair(ctypes.Structure):
                 ("d_slave", ctypes.c_void_p), ("s_nx", ctypes.c_int32), ("s_ny", ctypes.c_int32),
                 ("x_offset", ctypes.c_int32), ("y_offset", ctypes.c_int32), ("astretcha", ctypes.c_double),
                 ("locs", ctypes.c_void_p), ("nlocs", ctypes.c_int32), ("strip_len", ctypes.c_int32),
-                ("xsearch", ctypes.c_int32), ("ysearch", ctypes.c_int32), ("d_results", ctypes.c_void_p)]
+                ("xsearch", ctypes.c_int32), ("ysearch", ctypes.c_int32), ("d_results", ctypes.c_void_p),
+                ("d_features", ctypes.c_void_p)]
 
 
 class StackStats(ctypes.Structure):
@@ -112,6 +117,26 @@ def load(path: str | None = None):
     L.xcg_stack_autotune.argtypes = [ctypes.c_void_p, ctypes.POINTER(Pair), ctypes.c_int32, ctypes.c_void_p]
     L.xcg_stack_set_graph.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_stack_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(StackStats)]
+    L.xcg_set_features.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.xcg_refiner_create.restype = ctypes.c_int
+    L.xcg_refiner_create.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
+    L.xcg_refiner_destroy.argtypes = [ctypes.c_void_p]
+    for fn in ("xcg_refiner_set_params", "xcg_refiner_get_params"):
+        getattr(L, fn).restype = ctypes.c_int
+        getattr(L, fn).argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.xcg_refiner_forward.restype = ctypes.c_int
+    L.xcg_refiner_forward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                                      ctypes.c_int32, ctypes.c_void_p]
+    L.xcg_refiner_gradient.restype = ctypes.c_int
+    L.xcg_refiner_gradient.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                       ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+                                       ctypes.c_void_p]
+    L.xcg_refiner_train_step.restype = ctypes.c_int
+    L.xcg_refiner_train_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                         ctypes.c_float, ctypes.c_void_p]
+    L.xcg_correlate_device_refined.restype = ctypes.c_int
+    L.xcg_correlate_device_refined.argtypes = ([ctypes.c_void_p, ctypes.c_void_p] + L.xcg_correlate.argtypes[1:]
+                                               + [ctypes.c_float, ctypes.c_float, ctypes.c_void_p])
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
     _lib = L
@@ -178,6 +203,20 @@ class Context:
                                      locs.ctypes.data, len(locs), int(strip_len), out.ctypes.data))
         return out
 
+    def set_features(self, d_features: int | None):
+        """Also write each window's normalised 9x9 peak neighbourhood (device [nlocs][81])."""
+        self._L.xcg_set_features(self._h, d_features)
+
+    def correlate_device_refined(self, refiner: "Refiner", d_master: int, m_nx: int, m_ny: int, d_slave: int,
+                                 s_nx: int, s_ny: int, d_locs: int, nlocs: int, d_results: int, stream: int = 0,
+                                 x_offset=0, y_offset=0, astretcha=0.0, strip_len=0, max_sigma=0.08,
+                                 max_disagree=0.25):
+        """The correlation with the subpixel refiner where it is confident."""
+        _check(self._L.xcg_correlate_device_refined(self._h, refiner._h, d_master, m_nx, m_ny, d_slave, s_nx, s_ny,
+                                                    int(x_offset), int(y_offset), float(astretcha), d_locs, nlocs,
+                                                    int(strip_len), d_results, float(max_sigma),
+                                                    float(max_disagree), stream))
+
     def correlate_device(self, d_master: int, m_nx: int, m_ny: int, d_slave: int, s_nx: int, s_ny: int,
                          d_locs: int, nlocs: int, d_results: int, stream: int = 0, x_offset=0, y_offset=0,
                          astretcha=0.0, strip_len=0):
@@ -230,6 +269,53 @@ class Stack:
         s = StackStats()
         self._L.xcg_stack_get_stats(self._h, ctypes.byref(s))
         return s
+
+
+class Refiner:
+    """The subpixel refiner (xcg_refiner_*): parameters, CUDA training step,
+    FP32 and BF16 tensor-core forward passes."""
+
+    def __init__(self, device: int = 0, max_batch: int = 4096):
+        self._L = load()
+        h = ctypes.c_void_p()
+        _check(self._L.xcg_refiner_create(device, max_batch, ctypes.byref(h)))
+        self._h = h
+        self.max_batch = max_batch
+
+    def close(self):
+        if self._h:
+            self._L.xcg_refiner_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, theta: np.ndarray):
+        theta = np.ascontiguousarray(theta, dtype=np.float32)
+        assert theta.size == REFINER_NPARAM
+        _check(self._L.xcg_refiner_set_params(self._h, theta.ctypes.data))
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(REFINER_NPARAM, np.float32)
+        _check(self._L.xcg_refiner_get_params(self._h, out.ctypes.data))
+        return out
+
+    def forward(self, d_feat: int, n: int, d_out: int, tensor_cores: bool = True, stream: int = 0):
+        _check(self._L.xcg_refiner_forward(self._h, d_feat, n, d_out, 1 if tensor_cores else 0, stream))
+
+    def gradient(self, d_feat: int, d_target: int, n: int, stream: int = 0):
+        g = np.zeros(REFINER_NPARAM, np.float32)
+        out = np.zeros((n, 3), np.float32)
+        loss = ctypes.c_double()
+        _check(self._L.xcg_refiner_gradient(self._h, d_feat, d_target, n, g.ctypes.data, ctypes.byref(loss),
+                                            out.ctypes.data, stream))
+        return loss.value, g, out
+
+    def train_step(self, d_feat: int, d_target: int, n: int, lr: float, stream: int = 0):
+        _check(self._L.xcg_refiner_train_step(self._h, d_feat, d_target, n, float(lr), stream))
 
 
 def correlate_device_noalloc(p: Params, d_master: int, m_nx: int, m_ny: int, d_slave: int, s_nx: int, s_ny: int,

@@ -52,7 +52,8 @@ typedef struct {
 } xcg_loc;
 
 enum { XCG_FLAG_OOB = 1,        /* part of a patch fell outside its image and was zero-filled */
-       XCG_FLAG_NEXTREAD = 2 }; /* the 8x8 neighbourhood used the next window's first surface value */
+       XCG_FLAG_NEXTREAD = 2,   /* the 8x8 neighbourhood used the next window's first surface value */
+       XCG_FLAG_REFINED = 4 };  /* xfrac/yfrac come from the subpixel refiner, not the FFT interpolation */
 
 /* Per-location result. */
 typedef struct {
@@ -160,6 +161,7 @@ typedef struct {
     int32_t nlocs, strip_len;
     int32_t xsearch, ysearch;                    /* this pair's window geometry */
     xcg_result *d_results;                       /* DEVICE array of nlocs results */
+    float *d_features;                           /* DEVICE [nlocs][81] 9x9 neighbourhoods, or NULL */
 } xcg_pair;
 
 typedef struct {
@@ -186,6 +188,47 @@ void xcg_stack_set_graph(xcg_stack *st, int32_t enable);
  * (appended to the file named by XCG_TUNE_CACHE, read back by new buckets). */
 xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, void *stream);
 void xcg_stack_get_stats(const xcg_stack *st, xcg_stack_stats *out);
+
+/* Make later xcg_correlate_device calls on this context also write, per
+ * window, the 9x9 neighbourhood of the integer peak normalised by the surface
+ * maximum (DEVICE [nlocs][81]; NULL stops it): the subpixel refiner's input. */
+void xcg_set_features(xcg_ctx *ctx, float *d_features);
+
+/* ---- Subpixel refiner ----
+ * A small CNN (3 valid 3x3 convolutions of 32 channels, GELU, dense 64,
+ * dense 3; XCG_REFINER_NPARAM FP32 parameters) that reads the 9x9
+ * neighbourhood and predicts (fx, fy, s): the subpixel peak position in
+ * surface pixels (the xfrac/yfrac of highres_corr.cu:67-76) and the log
+ * variance of that estimate.  Trained by its own CUDA kernels (forward,
+ * backward, Adam).  No counterpart in the reference. */
+#define XCG_REFINER_NPARAM 37507
+typedef struct xcg_refiner xcg_refiner;
+/* max_batch: largest training/gradient batch (inference takes any size). */
+xcg_status xcg_refiner_create(int32_t device, int32_t max_batch, xcg_refiner **out);
+void xcg_refiner_destroy(xcg_refiner *r);
+/* Host parameter vector, FP32, in this order: W1 [32][1][3][3], b1,
+ * W2 [32][32][3][3], b2, W3, b3, F1 [64][288], c1, F2 [3][64], c2); resets Adam. */
+xcg_status xcg_refiner_set_params(xcg_refiner *r, const float *host_params);
+xcg_status xcg_refiner_get_params(xcg_refiner *r, float *host_params);
+/* d_out [n][3]; tensor_cores = 1: BF16 tensor-core inference kernel, 0: FP32 training forward. */
+xcg_status xcg_refiner_forward(xcg_refiner *r, const float *d_feat, int32_t n, float *d_out, int32_t tensor_cores,
+                               void *stream);
+/* Loss, parameter gradient and outputs of one batch (n <= max_batch), to host; synchronous. */
+xcg_status xcg_refiner_gradient(xcg_refiner *r, const float *d_feat, const float *d_target, int32_t n,
+                                float *host_grad, double *host_loss, float *host_out, void *stream);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on one batch; d_target [n][2] = (fx, fy). */
+xcg_status xcg_refiner_train_step(xcg_refiner *r, const float *d_feat, const float *d_target, int32_t n, float lr,
+                                  void *stream);
+/* The correlation with the refiner in place of the FFT interpolation where
+ * its predicted standard deviation is below max_sigma and it agrees with a
+ * 3-point parabola fit within max_disagree (both in surface pixels); those
+ * windows carry XCG_FLAG_REFINED, the others get the plain subpixel result. */
+xcg_status xcg_correlate_device_refined(xcg_ctx *ctx, xcg_refiner *r,
+                                        const void *d_master, int32_t m_nx, int32_t m_ny,
+                                        const void *d_slave, int32_t s_nx, int32_t s_ny,
+                                        int32_t x_offset, int32_t y_offset, double astretcha,
+                                        const xcg_loc *d_locs, int32_t nlocs, int32_t strip_len,
+                                        xcg_result *d_results, float max_sigma, float max_disagree, void *stream);
 
 /* Record CUDA events around every kernel launch (adds a synchronisation at
  * the end of each correlate call to read them). */

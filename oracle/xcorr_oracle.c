@@ -248,8 +248,8 @@ int xo_run(const xo_params *p, int precision, int format,
             md[k] = same_strip ? (precision == XO_F64 ? pow_quarter_f64(out[w + 1].corr0n)
                                                       : pow_quarter_f32(out[w + 1].corr0n)) : 0.0;
         }
-        if (precision == XO_F64) window_b_f64(p, md, r);
-        else window_b_f32(p, md, r);
+        if (precision == XO_F64) window_b_f64(p, md, r, NULL);
+        else window_b_f32(p, md, r, NULL);
     }
     free(mds);
     free(nexts);
@@ -335,4 +335,29 @@ void xo_surface(const xo_params *p, int precision, const float *pm_c, const floa
         free(c1); free(c2); free(w);
     }
     free(ints);
+}
+
+int xo_fine_surface(const xo_params *p, int precision, int format,
+                    const void *master, int m_nx, int m_ny, const void *slave, int s_nx, int s_ny,
+                    int x_offset, int y_offset, double astretcha, int x, int y,
+                    double *re_out, xo_result *r)
+{
+    if (!p || !re_out || !r) return 1;
+    prewarm(p);
+    const int n2 = p->n2x * p->n2y;
+    double md[256];
+    unsigned char nx[256];
+    float *pm = (float *)malloc(sizeof(float) * 2 * (size_t)p->npx * p->npy);
+    float *ps = (float *)malloc(sizeof(float) * 2 * (size_t)p->npx * p->npy);
+    int ishft = (int)((double)y * astretcha);
+    memset(r, 0, sizeof *r);
+    cut_patch(format, master, m_nx, m_ny, x - p->npx / 2, y - p->npy / 2, p->npx, p->npy, pm);
+    cut_patch(format, slave, s_nx, s_ny, x + x_offset - p->npx / 2, y + y_offset + ishft - p->npy / 2, p->npx, p->npy, ps);
+    if (precision == XO_F64) window_a_f64(p, pm, ps, r, md, nx);
+    else window_a_f32(p, pm, ps, r, md, nx);
+    for (int k = 0; k < n2; k++) if (nx[k]) md[k] = 0.0;
+    if (precision == XO_F64) window_b_f64(p, md, r, re_out);
+    else window_b_f32(p, md, r, re_out);
+    free(pm); free(ps);
+    return 0;
 }

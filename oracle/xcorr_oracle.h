@@ -65,6 +65,13 @@ int xo_run(const xo_params *p, int precision, int format,
            const int32_t *loc_xy, int nlocs, int strip_len, int nthreads,
            xo_result *out);
 
+/* One location run in full, also returning the interpolated real surface
+ * (ny2 x nx2 doubles) the subpixel argmax is taken over (no cross-window read). */
+int xo_fine_surface(const xo_params *p, int precision, int format,
+                    const void *master, int m_nx, int m_ny, const void *slave, int s_nx, int s_ny,
+                    int x_offset, int y_offset, double astretcha, int x, int y,
+                    double *re_out, xo_result *r);
+
 /* Stage-level views, for kernel parity tests. */
 /* One patch row range-interpolated by ri (xcorr.cu:237-250); in/out npx complex. */
 void xo_range_interp_row(int precision, int npx, int ri, const double *in_c, double *out_c);

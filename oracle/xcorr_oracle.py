@@ -60,6 +60,12 @@ def lib():
                                        ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
         L.xo_surface.argtypes = [ctypes.POINTER(XoParams), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                  ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.xo_fine_surface.restype = ctypes.c_int
+        L.xo_fine_surface.argtypes = [ctypes.POINTER(XoParams), ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_void_p]
         L.xo_argmax_ref.restype = ctypes.c_int64
         L.xo_argmax_ref.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
         _lib = L
@@ -134,3 +140,30 @@ def output_offsets(res: np.ndarray, ri: int, x_offset: int, y_offset: int, locs_
     xo = (res["xoff"].astype(f) / f(ri)) - (res["xfrac"].astype(f) / f(ri)) + f(x_offset)
     yo = res["yoff"].astype(f) - res["yfrac"].astype(f) + f(y_offset) + ishft.astype(f)
     return xo.astype(f), yo.astype(f)
+
+
+def fine_surface(p: XoParams, master, slave, x, y, x_offset=0, y_offset=0, astretcha=0.0, precision=F64):
+    """The interpolated real surface (ny2 x nx2) of one location, and its result."""
+    fmt = 1 if master.dtype == np.float32 else 0
+    master = np.ascontiguousarray(master)
+    slave = np.ascontiguousarray(slave)
+    ny2, nx2 = p.n2y * p.ifc, p.n2x * p.ifc
+    re = np.zeros((ny2, nx2), np.float64)
+    r = np.zeros(1, dtype=RESULT_DTYPE)
+    rc = lib().xo_fine_surface(ctypes.byref(p), precision, fmt, master.ctypes.data, master.shape[1], master.shape[0],
+                               slave.ctypes.data, slave.shape[1], slave.shape[0], int(x_offset), int(y_offset),
+                               float(astretcha), int(x), int(y), re.ctypes.data, r.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("xo_fine_surface failed")
+    return re, r[0]
+
+
+def near_tie(p: XoParams, master, slave, x, y, a, b, x_offset=0, y_offset=0, astretcha=0.0, rel=1e-5):
+    """True when fine peaks a and b (row, col) are neighbouring cells whose FP64
+    interpolated values agree within `rel` of the peak value: a tie that FP32
+    rounding in either implementation can break either way."""
+    if abs(a[0] - b[0]) > 1 or abs(a[1] - b[1]) > 1:
+        return False
+    re, _ = fine_surface(p, master, slave, x, y, x_offset, y_offset, astretcha)
+    va, vb = re[a[0], a[1]], re[b[0], b[1]]
+    return abs(va - vb) <= rel * max(abs(va), abs(vb))

@@ -267,7 +267,7 @@ static double XN(pow_quarter)(double v)
  * argmax of the real part (d_do_highres_corr highres_corr.cu:23-79,
  * d_fft_interpolate_2d_strip fft_interpolate_routines.cu:118-147,
  * h_reduceCr_strip conv_ampl_demean.cu:730-756). */
-static void XN(window_b)(const xo_params *p, const double *md, xo_result *r)
+static void XN(window_b)(const xo_params *p, const double *md, xo_result *r, double *re_out)
 {
     const int nx = p->n2x, ny = p->n2y, ifc = p->ifc;
     const int nx2 = nx * ifc, ny2 = ny * ifc;
@@ -284,6 +284,7 @@ static void XN(window_b)(const xo_params *p, const double *md, xo_result *r)
         XN(interp1d)(in, ny, ifc, colo);
         for (int Y = 0; Y < ny2; Y++) re[(size_t)Y * nx2 + X] = (double)colo[2 * Y];
     }
+    if (re_out) memcpy(re_out, re, sizeof(double) * (size_t)nx2 * ny2);
     double vmax;
     int64_t pk = xo_argmax_ref(re, (int64_t)nx2 * ny2, &vmax);
     r->fip = (int32_t)(pk / nx2);

