@@ -303,8 +303,6 @@ int main(int argc, char **argv)
 
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
-    void *m = xcli_read_slc(xc.data1_name, xc.m_nx, xc.m_ny, xc.format);
-    void *s = xcli_read_slc(xc.data2_name, xc.s_nx, xc.s_ny, xc.format);
     xcg_ctx *ctx = NULL;
     xcg_status st = xcg_create(&p, 0, 0, &ctx);
     if (st != XCG_OK) {
@@ -312,10 +310,18 @@ int main(int argc, char **argv)
         return 1;
     }
     xcg_result *res = (xcg_result *)calloc((size_t)xc.nlocs + 1, sizeof(xcg_result));
-    st = xcg_correlate(ctx, m, xc.m_nx, xc.m_ny, s, xc.s_nx, xc.s_ny, xc.x_offset, xc.y_offset, xc.astretcha,
-                       xc.loc, xc.nlocs, xc.nxl, res);
-    if (st != XCG_OK) {
-        fprintf(stderr, "xcorr: %s: %s\n", xcg_status_string(st), xcg_last_error());
+    void *m = NULL, *s = NULL;
+    if (getenv("XCORR_WHOLE_READ")) {
+        /* read both images whole, then one call over all locations */
+        m = xcli_read_slc(xc.data1_name, xc.m_nx, xc.m_ny, xc.format);
+        s = xcli_read_slc(xc.data2_name, xc.s_nx, xc.s_ny, xc.format);
+        st = xcg_correlate(ctx, m, xc.m_nx, xc.m_ny, s, xc.s_nx, xc.s_ny, xc.x_offset, xc.y_offset, xc.astretcha,
+                           xc.loc, xc.nlocs, xc.nxl, res);
+        if (st != XCG_OK) {
+            fprintf(stderr, "xcorr: %s: %s\n", xcg_status_string(st), xcg_last_error());
+            return 1;
+        }
+    } else if (xcli_correlate_streamed(&xc, ctx, res) != 0) {
         return 1;
     }
     for (int i = 0; i < xc.nlocs; i++) xcli_print_result(out, &xc, i, &res[i]);

@@ -49,5 +49,8 @@ void xcli_handle_prm(char **argv, xcli *xc);
 void xcli_get_locations(xcli *xc);
 void *xcli_read_slc(const char *path, int nx, int ny, int format);
 void xcli_print_result(FILE *f, const xcli *xc, int iloc, const xcg_result *r);
+/* Correlate every location while streaming both SLCs from disk in bands of
+ * lines (slc_ingest.c); returns 0 on success. */
+int xcli_correlate_streamed(const xcli *xc, xcg_ctx *ctx, xcg_result *host_results);
 
 #endif
