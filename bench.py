@@ -197,7 +197,7 @@ def run_ours(args):
     m, s = synth.make_pair(synth.PairSpec(**SPEC))
     locs = xg.grid(2048, 4096, 20, 50)
     nwin = len(locs)
-    ctx = xg.Context(xg.params(64, 64, 2, 1, 16), device=dev.index)
+    ctx = xg.Context(xg.params(64, 64, 2, 1, 16), device=dev.index, max_batch=args.max_batch)
     dm = torch.from_numpy(m).to(dev)
     ds = torch.from_numpy(s).to(dev)
     dl = torch.from_numpy(locs).to(dev)
@@ -256,7 +256,7 @@ def run_ours(args):
     # interpolation where it is confident (same workload, same timing rules)
     surrogate = None
     wpath = os.path.join(ROOT, "gmtsar-gpu_gb300", "refiner", "subpix_refiner.f32")
-    if os.path.exists(wpath):
+    if os.path.exists(wpath) and not args.no_surrogate:
         from xcorr_gb300 import refiner_train as rt
         ref = xg.Refiner(dev.index, max_batch=64)
         ref.set_params(rt.load_weights(wpath))
@@ -360,6 +360,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the refined-path measurement")
+    ap.add_argument("--max-batch", type=int, default=0,
+                    help="windows per scratch slot (0: library default); small values keep profiler captures small")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -166,6 +166,7 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *
     if (!c || !r || nlocs < 0 || (nlocs > 0 && (!d_master || !d_slave || !d_locs || !d_results))) return XCG_ERR_ARG;
     if (m_nx <= 0 || m_ny <= 0 || s_nx <= 0 || s_ny <= 0 || strip_len < 0) return XCG_ERR_ARG;
     if (!c->base.interp_flag) { xcg::set_last_error("the refined path needs interp_flag = 1"); return XCG_ERR_ARG; }
+    if (c->base.corr_mode != 2) { xcg::set_last_error("the refined path runs the frequency-domain mode only"); return XCG_ERR_UNSUPPORTED; }
     XCG_TRY(ck(cudaSetDevice(c->device), "cudaSetDevice"));
     memset(&c->stats, 0, sizeof c->stats);
     if (nlocs == 0) return XCG_OK;

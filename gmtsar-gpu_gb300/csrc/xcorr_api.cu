@@ -17,6 +17,7 @@
 
 #include "team_fft.cuh"
 #include "xcorr_gb300.h"
+#include "time_corr.cuh"
 #include "xcorr_kernels.cuh"
 #include "xcorr_ctx.cuh"
 
@@ -124,6 +125,7 @@ void xcg_default_params(xcg_params *p) {
     p->interp_factor = 16;
     p->n2x = 8; p->n2y = 8;
     p->format = 0;
+    p->corr_mode = 2;
 }
 
 static size_t per_window_bytes(const xcg::Plan &B) {
@@ -160,6 +162,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
     }
     if (p->n2x != 8 || p->n2y != 8) { g_last_error = "n2x = n2y = 8 only"; return XCG_ERR_UNSUPPORTED; }
     if (p->format != 0 && p->format != 1) { g_last_error = "format must be 0 or 1"; return XCG_ERR_ARG; }
+    if (p->corr_mode < 0 || p->corr_mode > 2) { g_last_error = "corr_mode must be 0 (-time), 1 (-time4) or 2"; return XCG_ERR_ARG; }
 
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -185,6 +188,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
     B.n2x = p->n2x; B.n2y = p->n2y;
     B.nx2 = B.n2x * B.ifc; B.ny2 = B.n2y * B.ifc;
     B.format = p->format;
+    B.corr_mode = p->corr_mode;
     B.nchunks = B.npx * B.npy / 1024;
     B.qpitch = B.npx / 2 + 16;
 
@@ -224,6 +228,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         B.kx = c->d_tables + o_kx;
         B.ky = c->d_tables + o_ky;
         XCG_CK_C(xcg::kernels_setup(B), "kernel attributes");
+        if (B.corr_mode < 2) XCG_CK_C(xcg::time_setup(B), "kernel attributes");
 
         // scratch: up to max_batch windows, at most 8 GiB or 40% of free memory
         const size_t pw = per_window_bytes(B);
@@ -402,10 +407,11 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
         Q.winref = ref0 ? ref0 + Q.win0 : nullptr;
         for (int k = 0; k < nk; k++) {
             if (c->profiling) cudaEventRecord(c->events[ei++], ss);
+            const bool tm = Q.corr_mode < 2;     // -time / -time4: full-search surface
             switch (k) {
                 case 0: launch_rows(Q, ss); break;
-                case 1: launch_cols(Q, ss); break;
-                case 2: launch_peak(Q, ss); break;
+                case 1: if (tm) launch_tcorr(Q, ss); else launch_cols(Q, ss); break;
+                case 2: if (tm) launch_tpeak(Q, ss); else launch_peak(Q, ss); break;
                 case 3: launch_subpix(Q, ss); break;
             }
             if (c->profiling) cudaEventRecord(c->events[ei++], ss);

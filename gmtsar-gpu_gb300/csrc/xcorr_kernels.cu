@@ -23,6 +23,10 @@
 #include "team_fft.cuh"
 #include "xcorr_kernels.cuh"
 
+#ifndef XCG_COLS_BLOCKS
+#define XCG_COLS_BLOCKS 5
+#endif
+
 namespace xcg {
 
 
@@ -101,17 +105,21 @@ __device__ __forceinline__ int slave_row_shift(const PairDev &pd, int y) {
 // for p = 0 that is the input sample x[q] itself.  So one forward FFT and
 // ri-1 inverse FFTs of length N give every kept sample.
 //
-// A team of T lanes owns one 1024-sample chunk (1024/N rows) of one window.
-// Rows live in registers in the team layout (lane l: samples l + T*m); the
-// next row's samples are loaded while the current one is transformed.
+// A warp owns one 1024-sample chunk (1024/N rows) of one window; its teams of
+// T lanes take the chunk's rows in turn, so the two rows that the reference's
+// first reduction level adds (t and t+512) go through the same team and their
+// sum is the only chunk-sum state kept in shared memory.  Rows live in
+// registers in the team layout (lane l: samples l + T*m); the next row's
+// samples are loaded while the current one is transformed.
 template <int N>
 __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_rows(Plan P) {
     constexpr int T = fft_lanes(N);
     constexpr int TPW = 32 / T;
     constexpr int PADN = fft_padded_len(N);
     constexpr int RPC = (N >= 1024) ? 1 : 1024 / N;     // rows per 1024-sample chunk
-    constexpr int H = RPC / 2;
-    constexpr int ACC = (N >= 1024) ? 1024 : 512;
+    constexpr int RPT = (N >= 1024) ? 1 : 2;            // rows per team: t and t+512
+    static_assert(RPT * TPW == RPC, "chunk rows");
+    constexpr int ACC = (N >= 1024) ? 1024 : 512;       // first-level sums per patch
     constexpr int TWL = fft_twiddle_len(N);
     constexpr int PER = N / T;
 
@@ -119,19 +127,20 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
     const int lane = l32 % T;
-    const int team = warp * TPW + l32 / T;
-    const int teams = blockDim.x / T;
-    char *tbase = reinterpret_cast<char *>(tw + TWL) +
-                  (size_t)team * (PADN * sizeof(float2) + 2 * N * sizeof(float) + 2 * ACC * sizeof(float));
+    const int tm = l32 / T;                             // team within the warp
+    const int team = warp * TPW + tm;
+    char *tbase = reinterpret_cast<char *>(tw + TWL) + (size_t)team * (PADN * sizeof(float2) + 2 * N * sizeof(float));
     float2 *ex = reinterpret_cast<float2 *>(tbase);
     float *rb = reinterpret_cast<float *>(ex + PADN);    // [2][N] amplitudes in natural order
-    float *acc = rb + 2 * N;                             // [2][ACC] chunk-sum rows (lane-private slots)
+    float *acc = reinterpret_cast<float *>(reinterpret_cast<char *>(tw + TWL) +
+                                           (size_t)(blockDim.x / T) * (PADN * sizeof(float2) + 2 * N * sizeof(float))) +
+                 (size_t)warp * 2 * ACC;                 // [2][ACC] first-level sums of the warp's chunk
 
     for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_row[i];
     __syncthreads();
 
     const int w = blockIdx.y;
-    const int c = blockIdx.x * teams + team;           // chunk (always < nchunks, see launcher)
+    const int c = blockIdx.x * (blockDim.x >> 5) + warp;  // chunk (always < nchunks, see launcher)
     const xcg_loc loc = P.locs[w];
     int local, pidx;
     const PairDev pd = pair_of(P, w, local, pidx);
@@ -211,17 +220,17 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     };
 
     uint32_t rawm[PER], raws[PER];
-    load_row(0, c * RPC, rawm);
+    load_row(0, c * RPC + tm, rawm);
 #pragma unroll 1
-    for (int ir = 0; ir < RPC; ir++) {
-        const int r = c * RPC + ir;
+    for (int ir = 0; ir < RPT; ir++) {
+        const int r = c * RPC + ir * TPW + tm;
 #pragma unroll 1
         for (int pt = 0; pt < 2; pt++) {
             uint32_t cur[PER];
 #pragma unroll
             for (int m = 0; m < PER; m++) cur[m] = pt ? raws[m] : rawm[m];
             if (pt == 0) load_row(1, r, raws);                   // in flight during the master row
-            else if (ir + 1 < RPC) load_row(0, r + 1, rawm);     // in flight during the slave row
+            else if (ir + 1 < RPT) load_row(0, r + TPW, rawm);   // in flight during the slave row
             amp_row(pt, r, cur);
         }
         __syncwarp();
@@ -230,6 +239,7 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         float *a1g = P.amp1 + ((size_t)w * npy + r) * N;
         const bool r2c = (r >= P.ysearch) && (r < P.ysearch + P.ny_corr);
         float *a2g = P.amp2c + ((size_t)w * P.ny_corr + (r - P.ysearch)) * P.nx_corr;
+        float *acc1 = acc + tm * N, *acc2 = acc + ACC + tm * N;
         float2 v[PER];
 #pragma unroll
         for (int m = 0; m < PER; m++) {
@@ -241,10 +251,10 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
             if (in) { mn2 = fminf(mn2, a2); mx2 = fmaxf(mx2, a2); }
             a1g[e] = a1;
             if (r2c && e >= P.xsearch && e < P.xsearch + P.nx_corr) a2g[e - P.xsearch] = a2;
-            // chunk sums in the reference's order: x[t] + x[t+512] first
-            if (H == 0) { acc[e] = a1; acc[ACC + e] = a2; }
-            else if (ir < H) { acc[ir * N + e] = a1; acc[ACC + ir * N + e] = a2; }
-            else { acc[(ir - H) * N + e] = acc[(ir - H) * N + e] + a1; acc[ACC + (ir - H) * N + e] = acc[ACC + (ir - H) * N + e] + a2; }
+            // first reduction level in the reference's order: x[t] + x[t+512],
+            // rows ir = 0 and 1 of this team
+            if (ir == 0) { acc1[e] = a1; acc2[e] = a2; }
+            else { acc1[e] = acc1[e] + a1; acc2[e] = acc2[e] + a2; }
         }
         team_fft_reg<N, -1>(v, ex, tw, lane);
         float2 *zg = P.zrow + ((size_t)w * npy + r) * N;
@@ -252,35 +262,33 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         for (int m = 0; m < PER; m++) zg[lane + T * m] = v[m];
         __syncwarp();
     }
-    {   // any lane of the team that read outside an image
-        const unsigned tmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (l32 - lane));
-        oob = (__ballot_sync(0xffffffffu, oob) & tmask) != 0u;
-    }
-    // remaining tree levels, strides ACC/2 .. 1: lane l holds t = l + T*q, so
-    // strides >= T are register-local and smaller ones are team shuffles
+    oob = __ballot_sync(0xffffffffu, oob) != 0u;      // any lane of the chunk's warp
+    // remaining tree levels over the warp's ACC first-level sums, strides
+    // ACC/2 .. 1: lane L holds t = L + 32*q, so strides >= 32 are
+    // register-local and smaller ones are warp shuffles
 #pragma unroll
     for (int pt = 0; pt < 2; pt++) {
-        float a[ACC / T];
+        float a[ACC / 32];
 #pragma unroll
-        for (int q = 0; q < ACC / T; q++) a[q] = acc[pt * ACC + lane + T * q];
+        for (int q = 0; q < ACC / 32; q++) a[q] = acc[pt * ACC + l32 + 32 * q];
 #pragma unroll
-        for (int s = ACC / (2 * T); s >= 1; s >>= 1)
+        for (int s = ACC / 64; s >= 1; s >>= 1)
 #pragma unroll
             for (int q = 0; q < s; q++) a[q] = a[q] + a[q + s];
         float x = a[0];
 #pragma unroll
-        for (int o = T / 2; o > 0; o >>= 1) x = x + __shfl_xor_sync(0xffffffffu, x, o);
-        if (lane == 0) P.part[((size_t)w * 2 + pt) * P.nchunks + c] = x;
+        for (int o = 16; o > 0; o >>= 1) x = x + __shfl_xor_sync(0xffffffffu, x, o);
+        if (l32 == 0) P.part[((size_t)w * 2 + pt) * P.nchunks + c] = x;
     }
-    if (lane == 0) P.oobmap[(size_t)w * P.nchunks + c] = oob ? 1 : 0;
+    if (l32 == 0) P.oobmap[(size_t)w * P.nchunks + c] = oob ? 1 : 0;
 #pragma unroll
-    for (int o = T / 2; o > 0; o >>= 1) {
+    for (int o = 16; o > 0; o >>= 1) {
         mn1 = fminf(mn1, __shfl_xor_sync(0xffffffffu, mn1, o));
         mx1 = fmaxf(mx1, __shfl_xor_sync(0xffffffffu, mx1, o));
         mn2 = fminf(mn2, __shfl_xor_sync(0xffffffffu, mn2, o));
         mx2 = fmaxf(mx2, __shfl_xor_sync(0xffffffffu, mx2, o));
     }
-    if (lane == 0) {
+    if (l32 == 0) {
         float *mm = P.minmax + (size_t)w * 4 * P.nchunks;
         mm[c] = mn1; mm[P.nchunks + c] = mx1; mm[2 * P.nchunks + c] = mn2; mm[3 * P.nchunks + c] = mx2;
     }
@@ -294,23 +302,29 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
 // (:111-139), applied here in the frequency domain: the master loses
 // m1*N*M at bin (0,0), the slave m2 times the DFT of its mask.
 // One team per column pair (kx, N-kx); the CTA stages the pairs' columns in
-// shared memory with coalesced row reads and writes the half spectrum back
-// row by row.
+// shared memory with coalesced row reads, each FFT uses its own column slot as
+// the exchange buffer (the column is in registers meanwhile), and the half
+// spectrum goes back row by row.
 template <int M>
-__global__ void __launch_bounds__(128, (M >= 1024) ? 2 : (M >= 512 ? 3 : 4)) k_cols(Plan P) {
-    constexpr int T = fft_lanes(M);
-    constexpr int PADM = fft_padded_len(M);
-    constexpr int CS = PADM + 1;
-    constexpr int CP = 128 / T;                // column pairs per CTA = teams
-    constexpr int TWL = fft_twiddle_len(M);
+struct ColsGeom {
+    static constexpr int T = fft_lanes(M);
+    static constexpr int PADM = fft_padded_len(M);
+    static constexpr int CS = PADM + 1;
+    static constexpr int CP = 128 / T;            // column pairs per CTA = teams
+    static constexpr int TWL = fft_twiddle_len(M);
+    static constexpr int BLOCKS = (M >= 1024) ? 2 : (M >= 512 ? 3 : XCG_COLS_BLOCKS);
+};
+
+template <int M>
+__global__ void __launch_bounds__(128, ColsGeom<M>::BLOCKS) k_cols(Plan P) {
+    using G = ColsGeom<M>;
+    constexpr int T = G::T, CS = G::CS, CP = G::CP, TWL = G::TWL;
     constexpr int PER = M / T;
 
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *cols = tw + TWL;                   // [2*CP][CS]
-    float2 *exb = cols + 2 * CP * CS;          // [CP][PADM]
-    double *sh = reinterpret_cast<double *>(exb + CP * PADM);   // m1, m2
-    float *pbuf = reinterpret_cast<float *>(sh + 2);             // [2][nchunks]
+    double *sh = reinterpret_cast<double *>(cols + 2 * CP * CS);   // m1, m2
 
     const int w = blockIdx.y, b = blockIdx.x;
     const int N = P.npx;
@@ -320,7 +334,6 @@ __global__ void __launch_bounds__(128, (M >= 1024) ? 2 : (M >= 512 ? 3 : 4)) k_c
     const int team = warp * (32 / T) + l32 / T;
 
     for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_col[i];
-    for (int i = threadIdx.x; i < 2 * P.nchunks; i += blockDim.x) pbuf[i] = P.part[(size_t)w * 2 * P.nchunks + i];
     {   // thread t stages slot t % (2CP) for rows t / (2CP) + k * 128/(2CP): all loads first
         constexpr int RSTEP = 128 / (2 * CP);
         constexpr int NLD = M / RSTEP;
@@ -339,20 +352,26 @@ __global__ void __launch_bounds__(128, (M >= 1024) ? 2 : (M >= 512 ? 3 : 4)) k_c
             for (int k = 0; k < BATCH; k++) cols[s * CS + fft_pad(row0 + (k0 + k) * RSTEP)] = t[k];
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {                      // means in the reference's order (:719-724)
+    if (warp == 0) {
+        // patch means (:719-724): the reference adds the FP32 chunk sums in
+        // double in index order; these partial sums are exact in double for
+        // any realistic patch (chunk sums of one patch span far fewer than 29
+        // binary orders), so a tree order gives the same bits
+        const float *pb = P.part + (size_t)w * 2 * P.nchunks;
         double s1 = 0.0, s2 = 0.0;
-        for (int i = 0; i < P.nchunks; i++) s1 += (double)pbuf[i];
-        for (int i = 0; i < P.nchunks; i++) s2 += (double)pbuf[P.nchunks + i];
-        s1 /= (double)(N * M);
-        s2 /= (double)(N * M);
-        sh[0] = s1; sh[1] = s2;
-        if (b == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
+        for (int i = l32; i < P.nchunks; i += 32) { s1 += (double)pb[i]; s2 += (double)pb[P.nchunks + i]; }
+        s1 = warp_sum_f64(s1);
+        s2 = warp_sum_f64(s2);
+        if (l32 == 0) {
+            s1 /= (double)(N * M);
+            s2 /= (double)(N * M);
+            sh[0] = s1; sh[1] = s2;
+            if (b == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
+        }
     }
     __syncthreads();
     const float dc1 = (float)(sh[0] * (double)N * (double)M);
     const float m2 = (float)sh[1];
-    float2 *ex = exb + team * PADM;
 
     const int kx = kx0 + team;
     float2 *a = cols + team * CS;
@@ -361,12 +380,14 @@ __global__ void __launch_bounds__(128, (M >= 1024) ? 2 : (M >= 512 ? 3 : 4)) k_c
     // partner column first, back into its slot (read below at -ky)
 #pragma unroll
     for (int m = 0; m < PER; m++) z[m] = pa[fft_pad(lane + T * m)];
-    team_fft_reg<M, -1>(z, ex, tw, lane);
+    __syncwarp();
+    team_fft_reg<M, -1>(z, pa, tw, lane);
 #pragma unroll
     for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
 #pragma unroll
     for (int m = 0; m < PER; m++) z[m] = a[fft_pad(lane + T * m)];
-    team_fft_reg<M, -1>(z, ex, tw, lane);
+    __syncwarp();
+    team_fft_reg<M, -1>(z, a, tw, lane);
 #pragma unroll
     for (int m = 0; m < PER; m++) a[fft_pad(lane + T * m)] = z[m];
     __syncwarp();
@@ -396,9 +417,9 @@ __global__ void __launch_bounds__(128, (M >= 1024) ? 2 : (M >= 512 ? 3 : 4)) k_c
             if ((kxx + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
             z[m] = pr;
         }
-        team_fft_reg<M, +1>(z, ex, tw, lane);
         float2 *dst = (o == 0) ? a : pa;
-        __syncwarp();
+        __syncwarp();                            // every lane has read a and pa before dst is reused
+        team_fft_reg<M, +1>(z, dst, tw, lane);
 #pragma unroll
         for (int m = 0; m < PER; m++) dst[fft_pad(lane + T * m)] = z[m];
         __syncwarp();
@@ -728,14 +749,13 @@ static size_t rows_smem() {
     constexpr int ACC = (N >= 1024) ? 1024 : 512;
     const int teams = 128 / T;
     return fft_twiddle_len(N) * sizeof(float2) +
-           (size_t)teams * (fft_padded_len(N) * sizeof(float2) + 2 * N * sizeof(float) + 2 * ACC * sizeof(float));
+           (size_t)teams * (fft_padded_len(N) * sizeof(float2) + 2 * N * sizeof(float)) +
+           (size_t)(128 / 32) * 2 * ACC * sizeof(float);
 }
 template <int M>
-static size_t cols_smem(int nchunks) {
-    constexpr int T = fft_lanes(M);
-    constexpr int CP = 128 / T;
-    return fft_twiddle_len(M) * sizeof(float2) + (size_t)2 * CP * (fft_padded_len(M) + 1) * sizeof(float2) +
-           (size_t)CP * fft_padded_len(M) * sizeof(float2) + 2 * sizeof(double) + 2 * nchunks * sizeof(float);
+static size_t cols_smem(int) {
+    using G = ColsGeom<M>;
+    return G::TWL * sizeof(float2) + (size_t)2 * G::CP * G::CS * sizeof(float2) + 2 * sizeof(double);
 }
 template <int N>
 static size_t peak_smem() {
@@ -790,13 +810,12 @@ cudaError_t kernels_setup(const Plan &P) {
 
 template <int N>
 static void launch_rows_t(const Plan &P, cudaStream_t s) {
-    const int teams = 128 / fft_lanes(N);
-    dim3 grid(P.nchunks / teams, P.nwin);
+    dim3 grid(P.nchunks / 4, P.nwin);          // one chunk per warp, 4 warps per CTA
     k_rows<N><<<grid, 128, rows_smem<N>(), s>>>(P);
 }
 template <int M>
 static void launch_cols_t(const Plan &P, cudaStream_t s) {
-    constexpr int CP = 128 / fft_lanes(M);
+    constexpr int CP = ColsGeom<M>::CP;
     dim3 grid((P.npx / 2) / CP, P.nwin);
     k_cols<M><<<grid, 128, cols_smem<M>(P.nchunks), s>>>(P);
 }

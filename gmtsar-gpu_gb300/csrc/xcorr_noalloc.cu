@@ -123,6 +123,7 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
     if (p->nx_corr != 2 * xs || p->ny_corr != 2 * ys)
         return fail(XCG_ERR_UNSUPPORTED, "nx_corr/ny_corr must be 2*xsearch/2*ysearch");
     if (!(p->ri == 1 || p->ri == 2 || p->ri == 4 || p->ri == 8)) return fail(XCG_ERR_ARG, "ri must be 1, 2, 4 or 8");
+    if (p->corr_mode != 2) return fail(XCG_ERR_UNSUPPORTED, "the allocation-free entry runs the frequency-domain mode only");
     if (p->interp_flag && !(p->interp_factor == 8 || p->interp_factor == 16 || p->interp_factor == 32 ||
                             p->interp_factor == 64))
         return fail(XCG_ERR_ARG, "interp_factor must be 8, 16, 32 or 64");

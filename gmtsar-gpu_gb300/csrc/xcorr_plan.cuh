@@ -31,6 +31,7 @@ struct Plan {
     int ri, log2ri;
     int interp_flag, ifc, n2x, n2y, nx2, ny2;
     int format;            // 0 complex int16, 1 float32 real
+    int corr_mode;         // 2 frequency domain; 0 -time, 1 -time4 full search
     int nchunks;           // 1024-sample chunks per patch (npx*npy/1024)
     int qpitch;            // row pitch (complex) of the half-spectrum rows: npx/2 + 16
 

@@ -212,6 +212,10 @@ extern "C" {
 xcg_status xcg_stack_create(const xcg_params *common, int32_t device, xcg_stack **out) {
     if (!common || !out) return XCG_ERR_ARG;
     *out = nullptr;
+    if (common->corr_mode != 2) {
+        xcg::set_last_error("stacks run the frequency-domain mode only");
+        return XCG_ERR_UNSUPPORTED;
+    }
     xcg_stack *st = new xcg_stack();
     st->common = *common;
     st->device = device;

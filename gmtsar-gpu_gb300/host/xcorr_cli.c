@@ -19,7 +19,7 @@ const char *XCLI_USAGE =
     "\nUsage: xcorr master.PRM slave.PRM [-time] [-real] [-freq] [-nx n] [-ny n] [-xsearch xs] [-ysearch ys]\n"
     "master.PRM     	PRM file for reference image\n"
     "slave.PRM     	 	PRM file of secondary image\n"
-    "-time      		use time cross-correlation (not available in this build)\n"
+    "-time      		use time cross-correlation\n"
     "-freq      		use frequency cross-correlation (default)\n"
     "-real      		read float numbers instead of complex numbers\n"
     "-noshift  		ignore ashift and rshift in prm file (set to 0)\n"
@@ -32,7 +32,7 @@ const char *XCLI_USAGE =
     "-ysearch ys		search window size in y (azimuth) direction (int power of 2 [32 64 128 256])\n"
     "-interp  factor    	interpolate correlation function by factor (int) [default, 16]\n"
     "-v			verbose\n"
-    "output: \n freq_xcorr.dat (default) \n"
+    "output: \n freq_xcorr.dat (default) \n time_xcorr.dat (if -time option))\n"
     "\nuse fitoffset.csh to convert output to PRM format\n"
     "\nExample:\n"
     "xcorr IMG-HH-ALPSRP075880660-H1.0__A.PRM IMG-HH-ALPSRP129560660-H1.0__A.PRM -nx 20 -ny 50 \n";
@@ -87,10 +87,12 @@ void xcli_parse_command_line(int na, char **a, xcli *xc)
         if (!strcmp(a[n], "-freq")) {
             xc->corr_flag = 2;
             fprintf(stderr, " using frequency cross correlation\n");
-        } else if (!strcmp(a[n], "-time") || !strcmp(a[n], "-time4")) {
-            fprintf(stderr, " %s: time-domain full search is not available in this build "
-                            "(the reference GPU build does not support it either, xcorr.cu:348)\n", a[n]);
-            exit(1);
+        } else if (!strcmp(a[n], "-time")) {
+            xc->corr_flag = 0;
+            fprintf(stderr, " using time cross correlation\n");
+        } else if (!strcmp(a[n], "-time4")) {
+            xc->corr_flag = 1;
+            fprintf(stderr, " using 4th power time cross correlation\n");
         } else if (!strcmp(a[n], "-real")) {
             xc->format = 1;
             fprintf(stderr, " no interpolation\n");
@@ -256,7 +258,10 @@ int main(int argc, char **argv)
     xcli_set_defaults(&xc);
     xcli_parse_command_line(argc, argv, &xc);
     xcli_handle_prm(argv, &xc);
-    strcpy(xc.filename, "freq_xcorr.dat");
+    /* xcorr.cu:467-469 */
+    if (xc.corr_flag == 0) strcpy(xc.filename, "time_xcorr.dat");
+    if (xc.corr_flag == 1) strcpy(xc.filename, "time_xcorr_Gatelli.dat");
+    if (xc.corr_flag == 2) strcpy(xc.filename, "freq_xcorr.dat");
     FILE *out = fopen(xc.filename, "w");
     if (!out) xcli_die("Can't open output file", xc.filename);
     xcli_get_locations(&xc);
@@ -300,6 +305,7 @@ int main(int argc, char **argv)
     p.interp_factor = xc.interp_factor;
     p.n2x = xc.n2x; p.n2y = xc.n2y;
     p.format = xc.format;
+    p.corr_mode = xc.corr_flag;
 
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);

@@ -26,7 +26,8 @@ EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_cre
            "xcg_get_stats", "xcg_stack_create", "xcg_stack_destroy", "xcg_stack_run", "xcg_stack_set_graph",
            "xcg_stack_autotune", "xcg_stack_get_stats", "xcg_set_features", "xcg_refiner_create",
            "xcg_refiner_destroy", "xcg_refiner_set_params", "xcg_refiner_get_params", "xcg_refiner_forward",
-           "xcg_refiner_gradient", "xcg_refiner_train_step", "xcg_correlate_device_refined")
+           "xcg_refiner_gradient", "xcg_refiner_train_step", "xcg_correlate_device_refined",
+           "xcg_fit_offsets", "xcg_tc_gemm_check")
 REFINER_NPARAM = 37507
 FLAG_REFINED = 4
 NOALLOC_SCRATCH_BYTES = 32 << 20
@@ -35,7 +36,7 @@ NOALLOC_SCRATCH_BYTES = 32 << 20
 class Params(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in
                 ("xsearch", "ysearch", "nx_corr", "ny_corr", "ri", "interp_flag", "interp_factor",
-                 "n2x", "n2y", "format")]
+                 "n2x", "n2y", "format", "corr_mode")]
 
 
 class Loc(ctypes.Structure):
@@ -57,6 +58,20 @@ class Stats(ctypes.Structure):
 
 
 KERNEL_NAMES = ("k_rows", "k_cols", "k_peak", "k_subpix")
+
+
+class FitAxis(ctypes.Structure):
+    """xcg_fit_axis: offset = shift + stretch*x + a_stretch*y."""
+    _fields_ = [("shift", ctypes.c_double), ("stretch", ctypes.c_double), ("a_stretch", ctypes.c_double),
+                ("sub_int", ctypes.c_double), ("rms", ctypes.c_double), ("weight", ctypes.c_double),
+                ("ishift", ctypes.c_int32), ("npts", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Fit(ctypes.Structure):
+    _fields_ = [("range", FitAxis), ("azimuth", FitAxis)]
 
 
 class Pair(ctypes.Structure):
@@ -137,6 +152,10 @@ def load(path: str | None = None):
     L.xcg_correlate_device_refined.restype = ctypes.c_int
     L.xcg_correlate_device_refined.argtypes = ([ctypes.c_void_p, ctypes.c_void_p] + L.xcg_correlate.argtypes[1:]
                                                + [ctypes.c_float, ctypes.c_float, ctypes.c_void_p])
+    L.xcg_fit_offsets.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                  ctypes.c_int32, ctypes.c_double, ctypes.c_float, ctypes.c_int32, ctypes.c_int32,
+                                  ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+    L.xcg_tc_gemm_check.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 4
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
     _lib = L
@@ -149,10 +168,12 @@ def _check(rc):
         raise XcgError(f"{L.xcg_status_string(rc).decode()}: {L.xcg_last_error().decode()}")
 
 
-def params(xsearch=64, ysearch=64, ri=2, interp_flag=1, interp_factor=16, fmt=0) -> Params:
-    """Parameters derived the way parse_xcorr_input.c:139-158 couples them."""
+def params(xsearch=64, ysearch=64, ri=2, interp_flag=1, interp_factor=16, fmt=0, corr_mode=2) -> Params:
+    """Parameters derived the way parse_xcorr_input.c:139-158 couples them.
+    corr_mode: 2 frequency domain (default), 0 -time, 1 -time4."""
     return Params(xsearch=xsearch, ysearch=ysearch, nx_corr=2 * xsearch, ny_corr=2 * ysearch, ri=ri,
-                  interp_flag=interp_flag, interp_factor=interp_factor, n2x=8, n2y=8, format=fmt)
+                  interp_flag=interp_flag, interp_factor=interp_factor, n2x=8, n2y=8, format=fmt,
+                  corr_mode=corr_mode)
 
 
 class Context:
@@ -327,6 +348,20 @@ def correlate_device_noalloc(p: Params, d_master: int, m_nx: int, m_ny: int, d_s
     _check(L.xcg_correlate_device_noalloc(ctypes.byref(p), d_master, m_nx, m_ny, d_slave, s_nx, s_ny,
                                           int(x_offset), int(y_offset), float(astretcha), d_locs, nlocs,
                                           int(strip_len), d_results, stream))
+
+
+def fit_offsets(d_results: int, d_locs: int, nlocs: int, d_out: int, ri=2, x_offset=0, y_offset=0, astretcha=0.0,
+                snr_min=20.0, npar_range=3, npar_azimuth=3, robust_iters=0, stream: int = 0):
+    """xcg_fit_offsets: the PRM offset model fitted on the device from a
+    device result array; d_out is a device buffer of sizeof(Fit) bytes."""
+    L = load()
+    _check(L.xcg_fit_offsets(d_results, d_locs, int(nlocs), int(ri), int(x_offset), int(y_offset), float(astretcha),
+                             float(snr_min), int(npar_range), int(npar_azimuth), int(robust_iters), d_out, stream))
+
+
+def tc_gemm_check(m_tiles: int, n_tile: int, k: int, n_total: int, d_a: int, d_b: int, d_c: int, stream: int = 0):
+    """xcg_tc_gemm_check: the split-FP16 tcgen05 GEMM engine on FP32 device matrices."""
+    _check(load().xcg_tc_gemm_check(m_tiles, n_tile, k, n_total, d_a, d_b, d_c, stream))
 
 
 def grid(m_nx, m_ny, nxl, nyl, xsearch=64, ysearch=64):

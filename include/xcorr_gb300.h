@@ -43,6 +43,8 @@ typedef struct {
     int32_t interp_factor;      /* subpixel factor: 8, 16 (default) or 32 */
     int32_t n2x, n2y;           /* peak neighbourhood, 8 x 8 (parse_xcorr_input.c:75-76) */
     int32_t format;             /* 0: complex int16 I/Q samples; 1: float32 real samples (-real) */
+    int32_t corr_mode;          /* 2: frequency domain (default, -freq); 0: -time, 1: -time4 full-search
+                                   time-domain correlation (do_time_int_xcorr.cu:146-189) */
 } xcg_params;
 
 /* A location: master pixel (range x, azimuth y) of the window centre,
@@ -229,6 +231,42 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *ctx, xcg_refiner *r,
                                         int32_t x_offset, int32_t y_offset, double astretcha,
                                         const xcg_loc *d_locs, int32_t nlocs, int32_t strip_len,
                                         xcg_result *d_results, float max_sigma, float max_disagree, void *stream);
+
+/* Affine fit of one pair's offsets, computed on the device from the result
+ * array: the step GMTSAR's fitoffset.csh performs on freq_xcorr.dat (named at
+ * xcorr.cu:52; the script is not in the reference sources) to produce the PRM
+ * parameters rshift/sub_int_r/stretch_r/a_stretch_r and ashift/sub_int_a/
+ * stretch_a/a_stretch_a.  Offsets are taken as print_results.c:37-38 forms
+ * them; locations with corr <= snr_min are left out.  Per axis the model is
+ * shift + stretch*x + a_stretch*y (npar 3), without a_stretch (npar 2), or a
+ * constant (npar 1).  robust_iters > 0: that many Tukey-biweight reweighted
+ * passes after the least-squares one. */
+typedef struct {
+    double shift;          /* constant term: shift + stretch*x + a_stretch*y */
+    double stretch;        /* per range pixel (x) */
+    double a_stretch;      /* per azimuth line (y) */
+    double sub_int;        /* shift - ishift */
+    double rms;            /* weighted rms residual of the final pass */
+    double weight;         /* sum of the final pass's weights */
+    int32_t ishift;        /* (int) shift: rshift / ashift */
+    int32_t npts;          /* locations passing snr_min */
+} xcg_fit_axis;
+typedef struct {
+    xcg_fit_axis range, azimuth;
+} xcg_fit;
+/* d_out: device pointer; asynchronous on stream. */
+xcg_status xcg_fit_offsets(const xcg_result *d_results, const xcg_loc *d_locs, int32_t nlocs, int32_t ri,
+                           int32_t x_offset, int32_t y_offset, double astretcha, float snr_min,
+                           int32_t npar_range, int32_t npar_azimuth, int32_t robust_iters, xcg_fit *d_out,
+                           void *stream);
+
+/* Diagnostic: the split-FP16 tensor-core GEMM engine of the precision form
+ * (tcgen05, FP32 accumulation in tensor memory) on caller matrices:
+ * C (m_tiles*128 x n_total) = A (m_tiles*128 x k) * B (k x n_total), all FP32
+ * row-major device arrays; (m_tiles, n_tile) one of (4, 128), (2, 144),
+ * (1, 256); k a multiple of 32, n_total of n_tile.  Synchronous. */
+xcg_status xcg_tc_gemm_check(int32_t m_tiles, int32_t n_tile, int32_t k, int32_t n_total,
+                             const float *d_a, const float *d_b, float *d_c, void *stream);
 
 /* Record CUDA events around every kernel launch (adds a synchronisation at
  * the end of each correlate call to read them). */

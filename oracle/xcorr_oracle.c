@@ -141,6 +141,75 @@ static double xo_half_sum_ref(const double *x, int64_t n)
     return acc;
 }
 
+/* Full-search time-domain correlation surface of the -time / -time4 modes
+ * (do_time_corr, do_time_int_xcorr.cu:146-189): for every lag (ioff, joff) in
+ * [-ysearch, ysearch) x [-xsearch, xsearch), row ic = ioff + ysearch, column
+ * jc = joff + xsearch, calc_time_corr (:30-68, mode 0) or calc_time_corr_hat
+ * (:103-144, mode 1) over the ny_corr x nx_corr window of the (int) demeaned
+ * amplitudes.  The long long sums are kept modulo 2^64, which is what the
+ * reference's signed arithmetic does on its platform when the fourth powers
+ * overflow. */
+static void time_surface(const xo_params *p, const int32_t *i1, const int32_t *i2, double *corr)
+{
+    const int N = p->npx;
+    for (int ic = 0; ic < p->nyc; ic++) {
+        const int ioff = ic - p->ysearch;
+        for (int jc = 0; jc < p->nxc; jc++) {
+            const int joff = jc - p->xsearch;
+            uint64_t num = 0, d1 = 0, d2 = 0;
+            for (int y = 0; y < p->ny_corr; y++) {
+                const int32_t *ar = i1 + (size_t)(p->ysearch + y + ioff) * N + joff + p->xsearch;
+                const int32_t *br = i2 + (size_t)(p->ysearch + y) * N + p->xsearch;
+                for (int x = 0; x < p->nx_corr; x++) {
+                    const uint64_t a = (uint64_t)(int64_t)ar[x], b = (uint64_t)(int64_t)br[x];
+                    if (p->corr_mode == 0) {
+                        num += a * b; d1 += a * a; d2 += b * b;
+                    } else {
+                        num += a * a * b * b; d1 += a * a * a * a; d2 += b * b * b * b;
+                    }
+                }
+            }
+            const double dd = 1.0 * (double)(int64_t)d1 * (double)(int64_t)d2;
+            double g;
+            if (p->corr_mode == 0) {
+                const double den = sqrt(dd);
+                g = (den == 0.0) ? 0.0 : 100.0 * fabs((double)(int64_t)num / den);
+            } else {
+                const double den = (double)sqrtl((long double)dd);
+                g = (den == 0.0) ? 0.0 : fabs((double)(int64_t)num / den);
+                g = (g <= 0.5) ? 0.0 : 100.0 * sqrt((g * 2.0) - 1.0);
+            }
+            corr[(size_t)ic * p->nxc + jc] = g;
+        }
+    }
+}
+
+/* The peak rule of do_time_corr (:160-177): scan ioff, then joff, and move
+ * the peak when |corr| exceeds the float-rounded running maximum. */
+static void time_peak(const xo_params *p, const double *corr, xo_result *r)
+{
+    float max_corr = -1.0f, ipeak = -9999.0f, jpeak = -9999.0f;
+    double vmax = 0.0;
+    for (int ic = 0; ic < p->nyc; ic++)
+        for (int jc = 0; jc < p->nxc; jc++) {
+            const double v = fabs(corr[(size_t)ic * p->nxc + jc]);
+            if (v > vmax) vmax = v;
+            if (v > max_corr) {
+                max_corr = (float)v;
+                jpeak = (float)(jc - p->xsearch);
+                ipeak = (float)(ic - p->ysearch);
+            }
+        }
+    r->xoff = -1 * jpeak;
+    r->yoff = -1 * ipeak;
+    r->corr = max_corr;
+    r->gamma = max_corr;
+    r->cmax = vmax;
+    r->ip = (int32_t)ipeak + p->ysearch;
+    r->jp = (int32_t)jpeak + p->xsearch;
+    r->corr0n = corr[0];
+}
+
 /* ---- per-precision bodies ---- */
 #define R float
 #define SFX f32

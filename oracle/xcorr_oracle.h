@@ -33,6 +33,7 @@ typedef struct {
     int interp_flag;       /* 1: subpixel refinement */
     int ifc;               /* interpolation factor (16) */
     int n2x, n2y;          /* peak neighbourhood (8 x 8, parse_xcorr_input.c:75-76) */
+    int corr_mode;         /* 2: frequency domain (default); 0: -time, 1: -time4 full search */
 } xo_params;
 
 /* flags */

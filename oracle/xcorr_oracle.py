@@ -21,7 +21,7 @@ F32, F64 = 32, 64
 class XoParams(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in
                 ("npx", "npy", "nxc", "nyc", "nx_corr", "ny_corr", "xsearch", "ysearch",
-                 "ri", "interp_flag", "ifc", "n2x", "n2y")]
+                 "ri", "interp_flag", "ifc", "n2x", "n2y", "corr_mode")]
 
 
 RESULT_DTYPE = np.dtype([
@@ -72,11 +72,12 @@ def lib():
     return _lib
 
 
-def params(xsearch=64, ysearch=64, ri=2, interp_flag=1, ifc=16, n2x=8, n2y=8) -> XoParams:
-    """Parameters as parse_xcorr_input.c:67-86,139-158 derives them from xsearch/ysearch."""
+def params(xsearch=64, ysearch=64, ri=2, interp_flag=1, ifc=16, n2x=8, n2y=8, corr_mode=2) -> XoParams:
+    """Parameters as parse_xcorr_input.c:67-86,139-158 derives them from xsearch/ysearch.
+    corr_mode: 2 frequency domain (default), 0 -time, 1 -time4."""
     return XoParams(npx=4 * xsearch, npy=4 * ysearch, nxc=2 * xsearch, nyc=2 * ysearch,
                     nx_corr=2 * xsearch, ny_corr=2 * ysearch, xsearch=xsearch, ysearch=ysearch,
-                    ri=ri, interp_flag=interp_flag, ifc=ifc, n2x=n2x, n2y=n2y)
+                    ri=ri, interp_flag=interp_flag, ifc=ifc, n2x=n2x, n2y=n2y, corr_mode=corr_mode)
 
 
 def run(p: XoParams, master: np.ndarray, slave: np.ndarray, locs: np.ndarray,

@@ -175,6 +175,32 @@ static void XN(surface)(const xo_params *p, R *c1, R *c2, double *corr)
     free(col);
 }
 
+/* 8x8 neighbourhood of the peak with the reference's flat bounds test
+ * (d_cppow_strip, conv_ampl_demean.cu:75-95): md = corr^0.25 around
+ * (xoff, yoff); next = 1 where it reads element nxc*nyc (the next window's
+ * first value). */
+static void XN(neighbourhood)(const xo_params *p, const double *corr, const xo_result *r, double *md,
+                              unsigned char *next)
+{
+    const int64_t ns = (int64_t)p->nxc * p->nyc;
+    int jc = (p->nxc / 2) - p->n2x / 2 - (int)r->xoff;
+    int ic = (p->nyc / 2) - p->n2y / 2 - (int)r->yoff;
+    for (int y = 0; y < p->n2y; y++) {
+        for (int x = 0; x < p->n2x; x++) {
+            int64_t k = (int64_t)(ic + y) * p->nxc + (jc + x);
+            md[y * p->n2x + x] = 0.0;
+            next[y * p->n2x + x] = 0;
+            if (k < 0 || k > ns) continue;
+            if (k == ns) { next[y * p->n2x + x] = 1; continue; }
+#if XO_IS_F32
+            md[y * p->n2x + x] = (double)powf((float)corr[k], 0.25f);
+#else
+            md[y * p->n2x + x] = pow(corr[k], 0.25);
+#endif
+        }
+    }
+}
+
 /* Phase A of one window: everything up to the normalised surface and the
  * 8x8 neighbourhood (d_assign_values xcorr.cu:261-292, d_do_freq_corr_strip
  * do_freq_xcorr.cu:123-200, d_calc_time_corr_strip do_time_int_xcorr.cu:71-100,
@@ -200,9 +226,18 @@ static void XN(window_a)(const xo_params *p, const float *pm, const float *ps, x
     }
     r->mean1 = XN(prep_patch)(p, c1, 0, i1, NULL);
     r->mean2 = XN(prep_patch)(p, c2, 1, i2, NULL);
+    const int64_t ns = (int64_t)p->nxc * p->nyc;
+    if (p->corr_mode < 2) {
+        /* -time / -time4: the full-search surface replaces the FFT surface and
+         * feeds the same 8x8 neighbourhood (no normalisation) */
+        time_surface(p, i1, i2, corr);
+        time_peak(p, corr, r);
+        XN(neighbourhood)(p, corr, r, md, next);
+        free(c1); free(c2); free(work); free(i1); free(i2); free(corr);
+        return;
+    }
     XN(surface)(p, c1, c2, corr);
 
-    const int64_t ns = (int64_t)p->nxc * p->nyc;
     double cmax;
     int64_t peak = xo_argmax_ref(corr, ns, &cmax);
     r->cmax = cmax;
@@ -234,23 +269,7 @@ static void XN(window_a)(const xo_params *p, const float *pm, const float *ps, x
     for (int64_t i = 0; i < ns; i++) corr[i] = corr[i] / msc;
     r->corr0n = corr[0];
 
-    /* 8x8 neighbourhood with the reference's flat bounds test (conv_ampl_demean.cu:82-93) */
-    int jc = (p->nxc / 2) - p->n2x / 2 - (int)r->xoff;
-    int ic = (p->nyc / 2) - p->n2y / 2 - (int)r->yoff;
-    for (int y = 0; y < p->n2y; y++) {
-        for (int x = 0; x < p->n2x; x++) {
-            int64_t k = (int64_t)(ic + y) * p->nxc + (jc + x);
-            md[y * p->n2x + x] = 0.0;
-            next[y * p->n2x + x] = 0;
-            if (k < 0 || k > ns) continue;
-            if (k == ns) { next[y * p->n2x + x] = 1; continue; }
-#if XO_IS_F32
-            md[y * p->n2x + x] = (double)powf((float)corr[k], 0.25f);
-#else
-            md[y * p->n2x + x] = pow(corr[k], 0.25);
-#endif
-        }
-    }
+    XN(neighbourhood)(p, corr, r, md, next);
     free(c1); free(c2); free(work); free(i1); free(i2); free(corr);
 }
 

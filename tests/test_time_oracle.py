@@ -1,0 +1,52 @@
+"""The -time / -time4 restatement in the oracle (do_time_corr,
+do_time_int_xcorr.cu:146-189).  The reference's GPU build runs these modes
+without data, so they have no golden vectors; they are pinned here to the
+frequency path, which is: the full-search surface at the frequency path's
+integer peak is the same calc_time_corr formula the frequency path evaluates
+there, so where both modes pick the same lag their correlation is identical,
+and on a clean pair both pick the true shift."""
+import numpy as np
+import pytest
+
+import golden_util as gu
+import xcorr_oracle as xo
+from xcorr_gb300 import synth
+from xcorr_gb300.synth import PairSpec
+
+
+@pytest.fixture(scope="module")
+def xs32():
+    g = gu.load("xs32")
+    m, s, locs, d, xoff, yoff, ast = gu.case_inputs("xs32", g)
+    return m, s, locs[:48], xoff, yoff, ast
+
+
+def test_time_mode_agrees_with_frequency_path(xs32):
+    m, s, locs, xoff, yoff, ast = xs32
+    f = xo.run(xo.params(32, 32), m, s, locs, xoff, yoff, ast, precision=xo.F32, strip_len=8)
+    t = xo.run(xo.params(32, 32, corr_mode=0), m, s, locs, xoff, yoff, ast, precision=xo.F32, strip_len=8)
+    same = (f["ip"] == t["ip"]) & (f["jp"] == t["jp"])
+    assert same.mean() > 0.9
+    # same lag, same formula, same ints: the correlation is identical
+    np.testing.assert_array_equal(t["corr"][same], f["corr"][same])
+    # the time surface's maximum is the reported peak value
+    np.testing.assert_array_equal(t["corr"], t["cmax"].astype(np.float32))
+
+
+def test_time4_clean_pair_finds_the_shift():
+    m, s = synth.make_pair(PairSpec(nx=768, ny=768, dx=2.0, dy=-3.0, noise_frac=0.002, seed=21))
+    locs = np.array([[384, 384], [320, 400], [448, 360]], np.int32)
+    t4 = xo.run(xo.params(32, 32, corr_mode=1), m, s, locs, precision=xo.F64)
+    t0 = xo.run(xo.params(32, 32, corr_mode=0), m, s, locs, precision=xo.F64)
+    np.testing.assert_array_equal(t4["xoff"], 4.0)          # 2 px at range interpolation 2
+    np.testing.assert_array_equal(t4["yoff"], -3.0)
+    np.testing.assert_array_equal(t0["xoff"], 4.0)
+    assert (t4["corr"] > 50).all() and (t0["corr"] > 90).all()
+
+
+def test_time4_noisy_pair_gives_zero_surface():
+    # the 4th-power estimate sqrt(2 r - 1) is defined only for r > 0.5; a noisy
+    # pair stays below and every lag scores 0, so the scan keeps the first lag
+    m, s = synth.make_pair(PairSpec(nx=512, ny=512, dx=2.3, dy=-1.6, noise_frac=0.2, seed=3))
+    r = xo.run(xo.params(32, 32, corr_mode=1), m, s, np.array([[256, 256]], np.int32), precision=xo.F64)
+    assert r["corr"][0] == 0.0 and r["xoff"][0] == 32.0 and r["yoff"][0] == 32.0
