@@ -134,15 +134,18 @@ def cpu_baseline(m, s, locs, target_s=8.0):
 
 
 def read_traffic():
-    """DRAM bytes per k_rows launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "k_rows_cfg1.md")
+    """DRAM bytes per window of a k_rows launch, from the committed ncu
+    summary (dram__bytes_read.sum + dram__bytes_write.sum of one captured
+    launch divided by its windows), if any."""
+    path = os.path.join(ROOT, "profiles", "k_rows_256_500win.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
         if line.startswith("traffic_bytes_per_launch:"):
             try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
+                f = line.split(":", 1)[1].split()
+                return float(f[0]) / float(f[1].lstrip("("))
+            except (ValueError, IndexError):
                 return None
     return None
 
@@ -243,10 +246,12 @@ def run_ours(args):
     # per-kernel times for the roofline (library events on the same stream)
     ctx.set_profiling(True)
     kms = [0.0] * 4
+    batches = 1
     for _ in range(max(3, min(args.steps, 20))):
         flush.zero_()
         step()
         st = ctx.stats()
+        batches = max(1, st.batches)
         for k in range(4):
             kms[k] += st.kernel_ms[k]
     ctx.set_profiling(False)
@@ -292,6 +297,52 @@ def run_ours(args):
                      "note": "rms as [range, azimuth] in original pixels over the 1000 windows"}
         ref.close()
 
+    # the precision form: the correlation's row/column DFTs as split-FP16
+    # tcgen05 matmuls (same workload and timing rules), compared with the
+    # FP32 path's results of the same windows
+    precision = None
+    if not args.no_precision_form:
+        drt = torch.zeros_like(dr)
+
+        def step_tc():
+            ctx.correlate_device(dm.data_ptr(), 2048, 4096, ds.data_ptr(), 2048, 4096, dl.data_ptr(), nwin,
+                                 drt.data_ptr(), sp, strip_len=20)
+        ctx.set_dft_form(1)
+        for _ in range(args.warmup):
+            flush.zero_()
+            step_tc()
+        torch.cuda.synchronize()
+        evt = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for i in range(args.steps):
+            flush.zero_()
+            evt[i][0].record(stream)
+            step_tc()
+            evt[i][1].record(stream)
+        torch.cuda.synchronize()
+        tc_ms = sum(a.elapsed_time(b) for a, b in evt)
+        ctx.set_profiling(True)
+        tkms = [0.0] * 6
+        for _ in range(nprof):
+            flush.zero_()
+            step_tc()
+            st = ctx.stats()
+            for k in range(6):
+                tkms[k] += st.kernel_ms[k]
+        ctx.set_profiling(False)
+        ctx.set_dft_form(0)
+        rp = np.frombuffer(dr.cpu().numpy().tobytes(), dtype=xg.RESULT_DTYPE)
+        rt_ = np.frombuffer(drt.cpu().numpy().tobytes(), dtype=xg.RESULT_DTYPE)
+        xp_, yp_ = xg.output_offsets(rp, 2, 0, 0, locs[:, 1], 0.0)
+        xt_, yt_ = xg.output_offsets(rt_, 2, 0, 0, locs[:, 1], 0.0)
+        precision = {"value": world * args.steps * nwin / (tc_ms / 1e3), "unit": UNIT,
+                     "ms_per_step": tc_ms / args.steps,
+                     "form": "split-FP16 (hi+lo) tcgen05 DFT matmuls, FP32 accumulation",
+                     "kernel_ms_per_step": {n: tkms[i] / nprof for i, n in enumerate(xg.TC_KERNEL_NAMES)},
+                     "same_integer_peak": float(np.mean((rt_["ip"] == rp["ip"]) & (rt_["jp"] == rp["jp"]))),
+                     "same_fine_peak": float(np.mean((rt_["fip"] == rp["fip"]) & (rt_["fjp"] == rp["fjp"]))),
+                     "max_offset_diff_px_vs_fp32": [float(np.max(np.abs(xt_ - xp_))), float(np.max(np.abs(yt_ - yp_)))],
+                     "median_corr_rel_diff_vs_fp32": float(np.median(np.abs(rt_["corr"] / rp["corr"] - 1)))}
+
     # end to end through the host-buffer entry point, pinned host memory
     pm = torch.from_numpy(m).pin_memory()
     ps = torch.from_numpy(s).pin_memory()
@@ -321,17 +372,21 @@ def run_ours(args):
         names = list(xg.KERNEL_NAMES)
         dom = int(np.argmax(kms))
         dom_name = names[dom]
-        avg_ms = kms[dom] / nprof
-        ach = fl[dom_name] * nwin / (avg_ms / 1e3) / 1e12
+        # one launch per batch: the step's windows split into `batches` launches
+        wpl = nwin / batches
+        avg_ms = kms[dom] / nprof / batches
+        ach = fl[dom_name] * wpl / (avg_ms / 1e3) / 1e12
         smax = peaks.get("sm_max_mhz", 2070.0)
         fp32_peak = 152 * 128 * 2 * smax * 1e6 / 1e12
-        traffic = read_traffic()
+        tpw = read_traffic()
+        traffic = tpw * wpl if tpw else None
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"bound": "fp32_simt", "kernel": dom_name, "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": ach / fp32_peak, "traffic": traffic,
                 "peak_source": "nominal FP32 SIMT rate, 152 SMs x 128 lanes x 2 flop at the measured max SM clock "
                                f"({smax:.0f} MHz, MEASURED_PEAKS.json); MEASURED_PEAKS.json has no FP32 figure",
-                "algorithmic": f"{fl[dom_name] / 1e6:.2f} MFLOP/window x {nwin} windows per launch",
+                "algorithmic": f"{fl[dom_name] / 1e6:.2f} MFLOP/window x {wpl:.0f} windows per launch "
+                               f"({batches} launches per {nwin}-window step)",
                 "avg_launch_ms": avg_ms,
                 "hbm": {"achieved": (traffic / (avg_ms / 1e3) / 1e9) if traffic else None, "peak": hbm_peak,
                         "unit": "GB/s", "frac": ((traffic / (avg_ms / 1e3) / 1e9) / hbm_peak) if traffic else None,
@@ -344,6 +399,7 @@ def run_ours(args):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(m.nbytes + s.nbytes + locs.nbytes),
                         "d2h_bytes_per_step": int(hostres.nbytes)},
                 "roofline": roof, "clocks": clk, "gpu_launches": launches, "surrogate": surrogate,
+                "precision_form": precision,
                 "wall_s_timed": wall}
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(m, s, locs)
@@ -361,6 +417,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the refined-path measurement")
+    ap.add_argument("--no-precision-form", action="store_true", help="skip the tensor-core DFT measurement")
     ap.add_argument("--max-batch", type=int, default=0,
                     help="windows per scratch slot (0: library default); small values keep profiler captures small")
     args = ap.parse_args()

@@ -1,9 +1,30 @@
-// Precision form of the correlation core on the tensor cores: split-FP16
-// GEMM engine checks (tc_gemm.cuh) exposed through a diagnostic C entry.
+// Precision form of the correlation core on the tensor cores.  The 2-D
+// correlation's forward row DFT, forward column DFT and the inverse column
+// DFT of the conjugate product (do_freq_xcorr.cu:90-117: cufftExecC2C forward
+// on both patches, d_mulaconjb, inverse) run as split-FP16 GEMMs on tcgen05
+// (tc_gemm.cuh) against DFT matrices embedded as real 2x2 blocks:
+//
+//   k_tc_rows  zrow[w][r][x]  -> zrow[w][r][kx]    A = row DFT (2N x 2N),  B = packed rows
+//   k_tc_cols  zrow[w][r][kx] -> zrow[w][ky][kx]   A = column DFT (2M x 2M), B = columns
+//   k_tc_inv   product of the two patches' spectra (Hermitian split, mean
+//              correction, (-1)^(kx+ky), as k_cols forms it) -> qspec rows of
+//              the surface band            A = inverse DFT rows (2 nyc x 2M)
+//
+// Operands are scaled by powers of two into the FP16 range before the hi/lo
+// split and scaled back in the epilogues (exact), so every buffer between the
+// stages holds the same quantity as in the FP32 path.  The range
+// interpolation (k_rows) and the inverse row transform with the peak search
+// (k_peak) stay FP32.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
+#include <cmath>
+#include <vector>
+
 #include "tc_gemm.cuh"
+#include "team_fft.cuh"
+#include "xcorr_ctx.cuh"
 #include "xcorr_gb300.h"
 
 namespace xcg {
@@ -35,12 +56,14 @@ __global__ void __launch_bounds__(128) k_tc_gemm_check(const uint8_t *__restrict
                                                         const float *__restrict__ B, int Ntot, float bscale,
                                                         float cscale, float *__restrict__ C, int *err) {
     const int n0 = blockIdx.x * NT;
-    auto loadB = [&](int k, int n) { return B[(size_t)k * Ntot + n0 + n] * bscale; };
+    auto loadB2 = [&](int k, int n) {
+        return make_float2(B[(size_t)k * Ntot + n0 + n] * bscale, B[(size_t)(k + 1) * Ntot + n0 + n] * bscale);
+    };
     auto epi = [&](int m, int c0, const float *v) {
 #pragma unroll
         for (int i = 0; i < 16; i++) C[(size_t)m * Ntot + n0 + c0 + i] = v[i] * cscale;
     };
-    tc::gemm_block<MT, NT, KC>(a_prep, K, loadB, epi, err);
+    tc::gemm_block<MT, NT, KC, false>(a_prep, K, loadB2, epi, err);
 }
 
 template <int MT, int NT, int KC>
@@ -71,8 +94,208 @@ xcg_status run_check(int K, int Ntot, const float *A, const float *B, float *C, 
     return XCG_OK;
 }
 
+constexpr float S_ROW = 1.0f / 16.0f;      // packed amplitudes (< 2^17) into the FP16 range
+constexpr float S_COL = 1.0f / 1024.0f;    // row spectra (< 2^8 * 2^17)
+
+// per-window bound of the column spectra, kept in the (not yet written)
+// first surface element of the window until k_peak runs
+__device__ __forceinline__ unsigned *ymax_slot(const Plan &P, int w) {
+    return reinterpret_cast<unsigned *>(P.surf + (size_t)w * P.nyc * P.nxc);
+}
+
+template <int N>
+__global__ void __launch_bounds__(128, 1) k_tc_rows(Plan P) {
+    const int w = blockIdx.y, r0 = blockIdx.x * 128;
+    float2 *z = P.zrow + (size_t)w * P.npy * N;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *ymax_slot(P, w) = 0u;
+    auto loadB2 = [&](int k, int n) {
+        const float2 v = z[(size_t)(r0 + n) * N + (k >> 1)];
+        return make_float2(v.x * S_ROW, v.y * S_ROW);
+    };
+    auto epi = [&](int m, int n0, const float *v) {
+        float *base = reinterpret_cast<float *>(z) + (m & 1);
+        const int kx = m >> 1;
+#pragma unroll
+        for (int i = 0; i < 16; i++) base[((size_t)(r0 + n0 + i) * N + kx) * 2] = v[i] * (1.0f / S_ROW);
+    };
+    tc::gemm_block<2 * N / 128, 128, 32, true>(P.tc_a_row, 2 * N, loadB2, epi, P.tc_err);
+}
+
+template <int M>
+__global__ void __launch_bounds__(128, 1) k_tc_cols(Plan P) {
+    const int N = P.npx;
+    const int w = blockIdx.y, kx0 = blockIdx.x * 128;
+    float2 *z = P.zrow + (size_t)w * M * N;
+    float ymax = 0.f;
+    auto loadB2 = [&](int k, int n) {
+        const float2 v = z[(size_t)(k >> 1) * N + kx0 + n];
+        return make_float2(v.x * S_COL, v.y * S_COL);
+    };
+    auto epi = [&](int m, int n0, const float *v) {
+        float *base = reinterpret_cast<float *>(z) + (m & 1);
+        const int ky = m >> 1;
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const float o = v[i] * (1.0f / S_COL);
+            base[((size_t)ky * N + kx0 + n0 + i) * 2] = o;
+            ymax = fmaxf(ymax, fabsf(o));
+        }
+    };
+    tc::gemm_block<2 * M / 128, 128, 32, false>(P.tc_a_col, 2 * M, loadB2, epi, P.tc_err);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ymax = fmaxf(ymax, __shfl_xor_sync(0xffffffffu, ymax, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(ymax_slot(P, w), __float_as_uint(ymax));
+}
+
+template <int M>
+__global__ void __launch_bounds__(128, 1) k_tc_inv(Plan P) {
+    const int N = P.npx;
+    const int w = blockIdx.x;
+    const float2 *z = P.zrow + (size_t)w * M * N;
+    __shared__ double msh[2];
+    __shared__ float ssh;
+    if (threadIdx.x < 32) {      // patch means (:719-724), as k_cols forms them
+        const int l32 = threadIdx.x;
+        const float *pb = P.part + (size_t)w * 2 * P.nchunks;
+        double s1 = 0.0, s2 = 0.0;
+        for (int i = l32; i < P.nchunks; i += 32) { s1 += (double)pb[i]; s2 += (double)pb[P.nchunks + i]; }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if (l32 == 0) {
+            s1 /= (double)(N * M);
+            s2 /= (double)(N * M);
+            msh[0] = s1; msh[1] = s2;
+            P.means[2 * w] = s1; P.means[2 * w + 1] = s2;
+            // |A1|, |A2| <= 2 |Y|max after the mean corrections: |product| < (2 sqrt2 ymax)^2
+            const float yb = 2.0f * 1.41421356f * __uint_as_float(*ymax_slot(P, w));
+            int e = 0;
+            frexpf(yb, &e);                        // yb < 2^e
+            ssh = ldexpf(1.0f, 13 - 2 * e);        // product * ssh < 2^13
+        }
+    }
+    __syncthreads();
+    const float dc1 = (float)(msh[0] * (double)N * (double)M);
+    const float m2 = (float)msh[1];
+    const float su = ssh;
+    auto loadB2 = [&](int k, int n) {
+        if (n > N / 2) return make_float2(0.f, 0.f);
+        const int ky = k >> 1;
+        const float2 z1 = z[(size_t)ky * N + n];
+        const float2 z2 = z[(size_t)((M - ky) & (M - 1)) * N + ((N - n) & (N - 1))];
+        // A1 = (z1 + conj z2)/2, A2 = (z1 - conj z2)/(2i)
+        float2 A1 = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+        float2 A2 = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+        if (n == 0 && ky == 0) A1.x -= dc1;
+        const float2 bm = cmulf(__ldg(P.box_x + n), __ldg(P.box_y + ky));
+        A2.x -= m2 * bm.x;
+        A2.y -= m2 * bm.y;
+        float2 pr = cmulf_conj(A1, A2);
+        if ((n + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
+        return make_float2(pr.x * su, pr.y * su);
+    };
+    auto epi = [&](int m, int n0, const float *v) {
+        float *q = reinterpret_cast<float *>(P.qspec + ((size_t)w * P.nyc + (m >> 1)) * P.qpitch) + (m & 1);
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            if (n0 + i <= N / 2) q[2 * (n0 + i)] = v[i] / su;
+    };
+    tc::gemm_block<M / 128, 144, 32, false>(P.tc_a_inv, 2 * M, loadB2, epi, P.tc_err);
+}
+
+// Real 2x2-block embedding of rows [row0, row0 + nrows) of an n-point DFT
+// matrix (sign -1 forward, +1 inverse): out[2r + c][2k + c'] with
+// (c, c') = (re, re) cos, (re, im) -sin*sign', (im, re) sin*sign', (im, im) cos.
+std::vector<float> dft_blocks(int n, int row0, int nrows, int sign) {
+    std::vector<float> a((size_t)2 * nrows * 2 * n);
+    for (int r = 0; r < nrows; r++)
+        for (int k = 0; k < n; k++) {
+            const long long ph = ((long long)(row0 + r) * k) % n;
+            const double th = 2.0 * M_PI * (double)ph / (double)n;
+            const double c = std::cos(th), sn = sign * std::sin(th);   // w = c + i sn
+            float *row_re = &a[(size_t)(2 * r) * 2 * n], *row_im = &a[(size_t)(2 * r + 1) * 2 * n];
+            row_re[2 * k] = (float)c;   row_re[2 * k + 1] = (float)-sn;
+            row_im[2 * k] = (float)sn;  row_im[2 * k + 1] = (float)c;
+        }
+    return a;
+}
+
 }  // namespace
+
+// Prepares the three DFT operands for a 256 x 256 geometry and switches the
+// context's plan to the precision form.
+xcg_status tc_enable(xcg_ctx *c) {
+    Plan &B = c->base;
+    if (B.npx != 256 || B.npy != 256) {
+        set_last_error("the precision form needs 128 x 128 windows (256 x 256 transforms)");
+        return XCG_ERR_UNSUPPORTED;
+    }
+    if (B.corr_mode != 2) {
+        set_last_error("the precision form applies to the frequency-domain mode");
+        return XCG_ERR_UNSUPPORTED;
+    }
+    if (B.tc_a_row) { B.tc_form = 1; return XCG_OK; }
+    const int N = B.npx, M = B.npy;
+    const std::vector<float> ar = dft_blocks(N, 0, N, -1), ac = dft_blocks(M, 0, M, -1),
+                             ai = dft_blocks(M, B.ysearch, B.nyc, +1);
+    const size_t br = tc::prepared_bytes<4, 128, 32>(2 * N), bc = tc::prepared_bytes<4, 128, 32>(2 * M),
+                 bi = tc::prepared_bytes<2, 144, 32>(2 * M);
+    uint8_t *prep = nullptr;
+    float *tmp = nullptr;
+    int *err = nullptr;
+    cudaError_t e = cudaMalloc(&prep, br + bc + bi);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp, ar.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(tmp, ar.data(), ar.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) { k_tc_prepare<4, 128, 32><<<256, 256>>>(tmp, 2 * N, 1.0f, prep); e = cudaDeviceSynchronize(); }
+    if (e == cudaSuccess) e = cudaMemcpy(tmp, ac.data(), ac.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) { k_tc_prepare<4, 128, 32><<<256, 256>>>(tmp, 2 * M, 1.0f, prep + br); e = cudaDeviceSynchronize(); }
+    if (e == cudaSuccess) e = cudaMemcpy(tmp, ai.data(), ai.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) { k_tc_prepare<2, 144, 32><<<256, 256>>>(tmp, 2 * M, 1.0f, prep + br + bc); e = cudaDeviceSynchronize(); }
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_tc_rows<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<4, 128, 32>::SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_tc_cols<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<4, 128, 32>::SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_tc_inv<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<2, 144, 32>::SMEM);
+    cudaFree(tmp);
+    if (e != cudaSuccess) {
+        cudaFree(prep);
+        cudaFree(err);
+        set_last_error(cudaGetErrorString(e));
+        return XCG_ERR_CUDA;
+    }
+    c->tc_prep = prep;
+    c->tc_err = err;
+    B.tc_a_row = prep;
+    B.tc_a_col = prep + br;
+    B.tc_a_inv = prep + br + bc;
+    B.tc_err = err;
+    B.tc_form = 1;
+    return XCG_OK;
+}
+
+void launch_tc_rows(const Plan &P, cudaStream_t s) {
+    k_tc_rows<256><<<dim3(P.npy / 128, P.nwin), 128, tc::GemmGeom<4, 128, 32>::SMEM, s>>>(P);
+}
+void launch_tc_cols(const Plan &P, cudaStream_t s) {
+    k_tc_cols<256><<<dim3(P.npx / 128, P.nwin), 128, tc::GemmGeom<4, 128, 32>::SMEM, s>>>(P);
+}
+void launch_tc_inv(const Plan &P, cudaStream_t s) {
+    k_tc_inv<256><<<P.nwin, 128, tc::GemmGeom<2, 144, 32>::SMEM, s>>>(P);
+}
+
 }  // namespace xcg
+
+extern "C" xcg_status xcg_set_dft_form(xcg_ctx *c, int32_t form) {
+    if (!c || form < 0 || form > 1) return XCG_ERR_ARG;
+    if (cudaSetDevice(c->device) != cudaSuccess) return XCG_ERR_CUDA;
+    if (form == 0) { c->base.tc_form = 0; return XCG_OK; }
+    return xcg::tc_enable(c);
+}
 
 extern "C" xcg_status xcg_tc_gemm_check(int32_t m_tiles, int32_t n_tile, int32_t k, int32_t n_total,
                                         const float *d_a, const float *d_b, float *d_c, void *stream) {

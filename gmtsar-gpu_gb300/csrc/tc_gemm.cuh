@@ -49,11 +49,13 @@ __host__ __device__ inline size_t prepared_bytes(int K) {
     return (size_t)(K / KC) * 2 * GemmGeom<MT, NT, KC>::A_TILE;
 }
 
-// Run the block.  loadB(k, n) -> float: B element (k, n) of this block (k in
-// [0, K), n in [0, NT)), already scaled into the FP16 range.  epi(m, n0, v):
-// the 16 accumulator values of row m (m in [0, MT*128)), columns n0..n0+15.
-template <int MT, int NT, int KC, class LoadB, class Epi>
-__device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, LoadB loadB, Epi epi, int *err) {
+// Run the block.  loadB2(k, n) -> float2: B elements (k, n) and (k+1, n) of
+// this block (k even in [0, K), n in [0, NT)), already scaled into the FP16
+// range.  K_FAST: consecutive threads take consecutive k pairs (B stored with
+// k contiguous), else consecutive n.  epi(m, n0, v): the 16 accumulator
+// values of row m (m in [0, MT*128)), columns n0..n0+15.
+template <int MT, int NT, int KC, bool K_FAST, class LoadB2, class Epi>
+__device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, LoadB2 loadB2, Epi epi, int *err) {
     using G = GemmGeom<MT, NT, KC>;
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     uint8_t *stage_base = tc_smem;
@@ -94,16 +96,20 @@ __device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, LoadB load
             bulk_g2s(st, a_prep + (size_t)c * 2 * G::A_TILE, 2 * G::A_TILE, &bar_a[s]);
         }
         copied = c + 1;
-        // B chunk: element (k, n) -> K-major core layout, hi and lo tiles
+        // B chunk: element pairs (k, k+1) of column n -> K-major core layout
+        // (adjacent halves of one 16-byte core row), hi and lo tiles
         __half *bhi = reinterpret_cast<__half *>(st + 2 * G::A_TILE);
         __half *blo = reinterpret_cast<__half *>(st + 2 * G::A_TILE + G::B_TILE);
-        for (int i = tid; i < NT * KC; i += 128) {
-            const int n = i % NT, k = i / NT;
-            __half h, l;
-            split_f16(loadB(c * KC + k, n), h, l);
-            const uint32_t off = kmajor_off(n, k, G::SBO) >> 1;
-            bhi[off] = h;
-            blo[off] = l;
+        for (int i = tid; i < NT * (KC / 2); i += 128) {
+            const int n = K_FAST ? i / (KC / 2) : i % NT;
+            const int k2 = K_FAST ? i % (KC / 2) : i / NT;
+            const float2 v = loadB2(c * KC + 2 * k2, n);
+            __half h0, l0, h1, l1;
+            split_f16(v.x, h0, l0);
+            split_f16(v.y, h1, l1);
+            const uint32_t off = kmajor_off(n, 2 * k2, G::SBO) >> 1;
+            *reinterpret_cast<__half2 *>(bhi + off) = __halves2half2(h0, h1);
+            *reinterpret_cast<__half2 *>(blo + off) = __halves2half2(l0, l1);
         }
         fence_async_smem();
         __syncthreads();

@@ -286,6 +286,8 @@ void xcg_destroy(xcg_ctx *c) {
     cudaFree(c->ref_feat);
     cudaFree(c->ref_pred);
     cudaFree(c->ref_skip);
+    cudaFree(c->tc_prep);
+    cudaFree(c->tc_err);
     for (cudaEvent_t ev : c->events) cudaEventDestroy(ev);
     for (int k = 0; k < 2; k++) {
         if (c->slot_stream[k]) { cudaStreamSynchronize(c->slot_stream[k]); cudaStreamDestroy(c->slot_stream[k]); }
@@ -375,7 +377,10 @@ static Plan with_slot(Plan P, size_t off) {
 }
 
 xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s) {
-    const int nk = P.interp_flag ? 4 : 3;
+    // launch slots: rows, columns, peak, subpixel; the precision form splits
+    // the column stage into three tensor-core DFT stages
+    const bool tcf = P.tc_form != 0;
+    const int nk = (tcf ? 6 : 4) - (P.interp_flag ? 0 : 1);
     if (c->profiling) {
         const size_t need = (size_t)nb * nk * 2;
         while (c->events.size() < need) {
@@ -408,11 +413,22 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
         for (int k = 0; k < nk; k++) {
             if (c->profiling) cudaEventRecord(c->events[ei++], ss);
             const bool tm = Q.corr_mode < 2;     // -time / -time4: full-search surface
-            switch (k) {
-                case 0: launch_rows(Q, ss); break;
-                case 1: if (tm) launch_tcorr(Q, ss); else launch_cols(Q, ss); break;
-                case 2: if (tm) launch_tpeak(Q, ss); else launch_peak(Q, ss); break;
-                case 3: launch_subpix(Q, ss); break;
+            if (tcf) {
+                switch (k) {
+                    case 0: launch_rows(Q, ss); break;
+                    case 1: launch_tc_rows(Q, ss); break;
+                    case 2: launch_tc_cols(Q, ss); break;
+                    case 3: launch_tc_inv(Q, ss); break;
+                    case 4: launch_peak(Q, ss); break;
+                    case 5: launch_subpix(Q, ss); break;
+                }
+            } else {
+                switch (k) {
+                    case 0: launch_rows(Q, ss); break;
+                    case 1: if (tm) launch_tcorr(Q, ss); else launch_cols(Q, ss); break;
+                    case 2: if (tm) launch_tpeak(Q, ss); else launch_peak(Q, ss); break;
+                    case 3: launch_subpix(Q, ss); break;
+                }
             }
             if (c->profiling) cudaEventRecord(c->events[ei++], ss);
             c->stats.launches++;
@@ -428,6 +444,7 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     c->stats.batches += nb;
     c->stats.batch_windows = maxw;
+    c->stats.nkernels = nk;
     if (c->profiling) {
         XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
         ei = 0;
@@ -482,6 +499,11 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     if (st != XCG_OK) return st;
     XCG_CK(cudaMemcpyAsync(results, c->d_res, (size_t)nlocs * sizeof(xcg_result), cudaMemcpyDeviceToHost, s), "copy results");
     XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (c->base.tc_form && c->tc_err) {     // a tensor-core wait that ran out leaves its block unwritten
+        int herr = 0;
+        XCG_CK(cudaMemcpy(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost), "read tensor-core status");
+        if (herr) { xcg::set_last_error("tensor-core stage: a wait ran out"); return XCG_ERR_CUDA; }
+    }
     return XCG_OK;
 }
 

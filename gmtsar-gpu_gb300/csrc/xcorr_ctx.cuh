@@ -38,6 +38,9 @@ struct xcg_ctx {
     float *ref_feat = nullptr, *ref_pred = nullptr;
     unsigned char *ref_skip = nullptr;
     int ref_cap = 0;
+    // precision form: prepared DFT operands and the tensor-core error flag
+    uint8_t *tc_prep = nullptr;
+    int *tc_err = nullptr;
     // profiling
     int profiling = 0;
     std::vector<cudaEvent_t> events;
@@ -52,4 +55,9 @@ Plan ctx_plan(const xcg_ctx *c);
 // window arrays in P (locs, winref), b < nbatch; updates the context stats.
 xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nbatch, cudaStream_t s);
 void set_last_error(const char *msg);
+// precision form (tc_dft.cu)
+xcg_status tc_enable(xcg_ctx *c);
+void launch_tc_rows(const Plan &P, cudaStream_t s);
+void launch_tc_cols(const Plan &P, cudaStream_t s);
+void launch_tc_inv(const Plan &P, cudaStream_t s);
 }  // namespace xcg

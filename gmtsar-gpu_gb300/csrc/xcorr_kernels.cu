@@ -256,7 +256,8 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
             if (ir == 0) { acc1[e] = a1; acc2[e] = a2; }
             else { acc1[e] = acc1[e] + a1; acc2[e] = acc2[e] + a2; }
         }
-        team_fft_reg<N, -1>(v, ex, tw, lane);
+        // the precision form transforms the packed rows on the tensor cores
+        if (!P.tc_form) team_fft_reg<N, -1>(v, ex, tw, lane);
         float2 *zg = P.zrow + ((size_t)w * npy + r) * N;
 #pragma unroll
         for (int m = 0; m < PER; m++) zg[lane + T * m] = v[m];

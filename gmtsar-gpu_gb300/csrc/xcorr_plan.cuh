@@ -32,6 +32,13 @@ struct Plan {
     int interp_flag, ifc, n2x, n2y, nx2, ny2;
     int format;            // 0 complex int16, 1 float32 real
     int corr_mode;         // 2 frequency domain; 0 -time, 1 -time4 full search
+    // precision form: the correlation's row/column DFTs as split-FP16
+    // tensor-core matmuls (tc_dft.cu); 0 = FP32 SIMT FFTs
+    int tc_form;
+    const uint8_t *tc_a_row;   // prepared forward DFT operand for the rows (npx)
+    const uint8_t *tc_a_col;   // forward DFT operand for the columns (npy)
+    const uint8_t *tc_a_inv;   // inverse DFT rows of the surface band (nyc x npy)
+    int *tc_err;               // raised when a tensor-core wait ran out
     int nchunks;           // 1024-sample chunks per patch (npx*npy/1024)
     int qpitch;            // row pitch (complex) of the half-spectrum rows: npx/2 + 16
 

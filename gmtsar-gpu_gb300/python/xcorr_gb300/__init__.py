@@ -27,7 +27,7 @@ EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_cre
            "xcg_stack_autotune", "xcg_stack_get_stats", "xcg_set_features", "xcg_refiner_create",
            "xcg_refiner_destroy", "xcg_refiner_set_params", "xcg_refiner_get_params", "xcg_refiner_forward",
            "xcg_refiner_gradient", "xcg_refiner_train_step", "xcg_correlate_device_refined",
-           "xcg_fit_offsets", "xcg_tc_gemm_check")
+           "xcg_fit_offsets", "xcg_tc_gemm_check", "xcg_set_dft_form")
 REFINER_NPARAM = 37507
 FLAG_REFINED = 4
 NOALLOC_SCRATCH_BYTES = 32 << 20
@@ -54,10 +54,12 @@ RESULT_DTYPE = np.dtype([
 
 class Stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64), ("batches", ctypes.c_int32), ("batch_windows", ctypes.c_int32),
-                ("kernel_ms", ctypes.c_double * 4), ("scratch_bytes", ctypes.c_size_t)]
+                ("kernel_ms", ctypes.c_double * 8), ("scratch_bytes", ctypes.c_size_t),
+                ("nkernels", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 KERNEL_NAMES = ("k_rows", "k_cols", "k_peak", "k_subpix")
+TC_KERNEL_NAMES = ("k_rows", "k_tc_rows", "k_tc_cols", "k_tc_inv", "k_peak", "k_subpix")
 
 
 class FitAxis(ctypes.Structure):
@@ -156,6 +158,7 @@ def load(path: str | None = None):
                                   ctypes.c_int32, ctypes.c_double, ctypes.c_float, ctypes.c_int32, ctypes.c_int32,
                                   ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
     L.xcg_tc_gemm_check.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 4
+    L.xcg_set_dft_form.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
     _lib = L
@@ -205,6 +208,10 @@ class Context:
 
     def set_profiling(self, on: bool):
         self._L.xcg_set_profiling(self._h, 1 if on else 0)
+
+    def set_dft_form(self, form: int):
+        """0: FP32 SIMT FFTs (default); 1: split-FP16 tensor-core DFTs (precision form)."""
+        _check(self._L.xcg_set_dft_form(self._h, int(form)))
 
     def stats(self) -> Stats:
         s = Stats()

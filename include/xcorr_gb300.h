@@ -81,8 +81,13 @@ typedef struct {
     int64_t launches;          /* kernels launched by this library */
     int32_t batches;
     int32_t batch_windows;     /* windows per batch */
-    double kernel_ms[4];       /* rows, columns, peak, subpixel: summed CUDA-event time when profiling */
+    double kernel_ms[8];       /* per launch slot, summed CUDA-event time when profiling: rows, columns,
+                                  peak, subpixel (frequency domain); rows, surface, peak, subpixel (-time);
+                                  rows, row DFT, column DFT, product + inverse column DFT, peak, subpixel
+                                  (tensor-core precision form) */
     size_t scratch_bytes;      /* device scratch held by the context */
+    int32_t nkernels;          /* launch slots used in kernel_ms */
+    int32_t pad;
 } xcg_stats;
 
 const char *xcg_status_string(xcg_status s);
@@ -259,6 +264,14 @@ xcg_status xcg_fit_offsets(const xcg_result *d_results, const xcg_loc *d_locs, i
                            int32_t x_offset, int32_t y_offset, double astretcha, float snr_min,
                            int32_t npar_range, int32_t npar_azimuth, int32_t robust_iters, xcg_fit *d_out,
                            void *stream);
+
+/* DFT form of the frequency-domain path: 0 (default) FP32 SIMT team FFTs; 1
+ * the precision form, in which the forward row and column DFTs of the 2-D
+ * correlation and the inverse column DFT of the product run as split-FP16
+ * (hi + lo) tensor-core matmuls with FP32 accumulation (tcgen05), the range
+ * interpolation and the inverse row transform staying FP32.  Form 1 needs
+ * 128 x 128 windows (xsearch = ysearch = 64, 256 x 256 transforms). */
+xcg_status xcg_set_dft_form(xcg_ctx *ctx, int32_t form);
 
 /* Diagnostic: the split-FP16 tensor-core GEMM engine of the precision form
  * (tcgen05, FP32 accumulation in tensor memory) on caller matrices:

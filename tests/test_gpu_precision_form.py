@@ -1,0 +1,64 @@
+"""The precision form (split-FP16 tcgen05 DFTs for the correlation's row and
+column transforms) on the 128x128-window golden case, against the
+reference's own outputs, the FP32 SIMT path and the FP64 oracle.  Split FP16
+carries about 22 bits per operand, so the surface differs from the FP32
+path's at the 1e-6 level: integer peaks must match the reference except
+where the FP64 oracle itself calls a near-tie, and the subpixel offsets must
+stay within the reference's 0.01 px of the FP32 path."""
+import numpy as np
+import pytest
+
+import golden_util as gu
+import xcorr_gb300 as xg
+import xcorr_oracle as xo
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cfg1():
+    g = gu.load("cfg1")
+    m, s, locs, d, xoff, yoff, ast = gu.case_inputs("cfg1", g)
+    p = xg.params(64, 64)
+    with xg.Context(p) as ctx:
+        r32 = ctx.correlate(m, s, locs, xoff, yoff, ast, strip_len=d["nxl"])
+        ctx.set_dft_form(1)
+        rtc = ctx.correlate(m, s, locs, xoff, yoff, ast, strip_len=d["nxl"])
+        ctx.set_dft_form(0)
+        r32b = ctx.correlate(m, s, locs, xoff, yoff, ast, strip_len=d["nxl"])
+    return g, m, s, locs, d, r32, rtc, r32b
+
+
+def test_switching_back_restores_the_fp32_path(cfg1):
+    g, m, s, locs, d, r32, rtc, r32b = cfg1
+    assert r32.tobytes() == r32b.tobytes()
+
+
+def test_precision_form_matches_reference(cfg1):
+    g, m, s, locs, d, r32, rtc, _ = cfg1
+    ip, jp = g["col"]("ip").astype(np.int32), g["col"]("jp").astype(np.int32)
+    bad = np.where((rtc["ip"] != ip) | (rtc["jp"] != jp))[0]
+    assert len(bad) <= 2, bad
+    same = (rtc["fip"] == r32["fip"]) & (rtc["fjp"] == r32["fjp"])
+    assert same.mean() >= 0.99, same.mean()
+    xo_t, yo_t = xg.output_offsets(rtc, 2, 0, 0, locs[:, 1], 0.0)
+    xo_f, yo_f = xg.output_offsets(r32, 2, 0, 0, locs[:, 1], 0.0)
+    assert np.max(np.abs(xo_t - xo_f)) <= 0.0625 and np.mean(np.abs(xo_t - xo_f) <= 0.01) >= 0.99
+    rel = np.abs(rtc["corr"].astype(np.float64) - r32["corr"]) / r32["corr"]
+    assert np.median(rel) < 1e-5 and rel.max() < 1e-3, (np.median(rel), rel.max())
+    assert np.max(np.abs(rtc["cmax"] / r32["cmax"] - 1)) < 1e-4
+
+
+def test_precision_form_error_against_fp64(cfg1):
+    """Both forms' offsets against the FP64 oracle, reported side by side."""
+    g, m, s, locs, d, r32, rtc, _ = cfg1
+    sub = np.arange(0, len(locs), 10)
+    o = xo.run(xo.params(64, 64), m, s, locs[sub], precision=xo.F64, strip_len=0)
+    xo_o, yo_o = xg.output_offsets(o, 2, 0, 0, locs[sub, 1], 0.0)
+    out = {}
+    for name, r in (("fp32", r32), ("split_fp16_tc", rtc)):
+        x, y = xg.output_offsets(r[sub], 2, 0, 0, locs[sub, 1], 0.0)
+        out[name] = (float(np.sqrt(np.mean((x - xo_o) ** 2))), float(np.sqrt(np.mean((y - yo_o) ** 2))))
+    print("rms offset error vs FP64 oracle [range, azimuth] px:", out)
+    assert out["split_fp16_tc"][0] <= out["fp32"][0] + 0.01
+    assert out["split_fp16_tc"][1] <= out["fp32"][1] + 0.01
