@@ -150,6 +150,140 @@ def read_traffic():
     return None
 
 
+def _timed(step, flush, stream, steps, warmup):
+    """Device time (ms) of `steps` calls of step(), L2 flushed before each."""
+    import torch
+    for _ in range(warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev)
+
+
+def run_frame(args):
+    """Full-frame workload: 10240 x 30720 complex-int16 pair with the shift
+    field dx = 2.1 + 1e-5 x - 3e-6 y, dy = -4.7 + 2e-6 x + 8e-6 y at 20 dB
+    SNR, 100 x 400 = 40,000 windows of 256 x 256 (512 x 512 transforms)."""
+    import torch
+    import xcorr_gb300 as xg
+    from xcorr_gb300 import synth
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t0 = time.perf_counter()
+    m, s, _ = synth.make_pair_varying(10240, 30720, synth.cfg2_shift, noise_frac=0.01, seed=2, device=dev)
+    gen_s = time.perf_counter() - t0
+    locs = xg.grid(10240, 30720, 100, 400, 128, 128)
+    nwin = len(locs)
+    ctx = xg.Context(xg.params(128, 128), device=dev.index, max_batch=args.max_batch)
+    dm, ds = torch.from_numpy(m).to(dev), torch.from_numpy(s).to(dev)
+    dl = torch.from_numpy(locs).to(dev)
+    dr = torch.zeros((nwin, xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        ctx.correlate_device(dm.data_ptr(), 10240, 30720, ds.data_ptr(), 10240, 30720, dl.data_ptr(), nwin,
+                             dr.data_ptr(), stream.cuda_stream, strip_len=100)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    ms = _timed(step, flush, stream, args.steps, args.warmup)
+    clk = clocks.stop()
+    ctx.set_profiling(True)
+    flush.zero_()
+    step()
+    st = ctx.stats()
+    ctx.set_profiling(False)
+    # end to end through the host entry point (2.5 GB of images in per call)
+    pm, ps = torch.from_numpy(m).pin_memory(), torch.from_numpy(s).pin_memory()
+    ctx.correlate(pm.numpy(), ps.numpy(), locs, strip_len=100)
+    t1 = time.perf_counter()
+    ctx.correlate(pm.numpy(), ps.numpy(), locs, strip_len=100)
+    e2e_s = time.perf_counter() - t1
+    line = {"metric": "xcorr windows/s, full frame, 256^2 windows (512^2 FFT)", "value": args.steps * nwin / (ms / 1e3),
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "full frame", "image": "10240x30720 complex int16, varying shift, 20 dB",
+                       "windows": nwin, "xsearch": 128, "ysearch": 128, "range_interp": 2, "interp": 16,
+                       "l2": "flushed between steps (256 MB write)", "generation_s": gen_s},
+            "kernel_ms_per_step": {n: st.kernel_ms[i] for i, n in enumerate(xg.KERNEL_NAMES)},
+            "batches_per_step": st.batches,
+            "e2e": {"value": nwin / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(m.nbytes + s.nbytes + locs.nbytes),
+                    "d2h_bytes_per_step": int(nwin * xg.RESULT_DTYPE.itemsize), "timer": "host wall clock"},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+def run_stack(args):
+    """Stack workload: 32 pairs from 2048 x 4096 to 10240 x 30720, integer
+    shifts uniform in [-8, 8] px, SNR uniform in 5-30 dB, window sizes mixed
+    from {64, 128, 256} (xsearch 32/64/128), 500-40,000 locations per pair,
+    all correlated by one stack call (graph-captured, batch sizes autotuned)."""
+    import torch
+    import xcorr_gb300 as xg
+    dev = torch.device("cuda", torch.cuda.current_device())
+    rng = np.random.default_rng(4)
+    sizes = [(2048, 4096), (4096, 8192), (6144, 15360), (8192, 22528), (10240, 30720)]
+    g = torch.Generator(device=dev).manual_seed(4)
+    items, pairs, total = [], [], 0
+    t0 = time.perf_counter()
+    for i in range(32):
+        nx, ny = sizes[rng.integers(len(sizes))]
+        xs = int(rng.choice([32, 64, 128]))
+        n = int(rng.integers(500, 40001))
+        need = 6 * xs + 8
+        nxl = max(1, min(int(np.sqrt(n * nx / ny)), (nx - need) // 4))
+        nyl = max(1, min(n // nxl, (ny - need) // 2))
+        dx, dy = (int(v) for v in rng.integers(-8, 9, 2))
+        snr = rng.uniform(5, 30)
+        m = torch.randn((ny, nx, 2), generator=g, device=dev).mul_(1000).round_().clamp_(-32768, 32767)
+        sl = torch.roll(m, shifts=(dy, dx), dims=(0, 1))
+        sl = sl + torch.randn((ny, nx, 2), generator=g, device=dev).mul_(1000 * 10 ** (-snr / 20))
+        dm = m.to(torch.int16)
+        ds = sl.round_().clamp_(-32768, 32767).to(torch.int16)
+        del m, sl
+        locs = xg.grid(nx, ny, nxl, nyl, xs, xs)
+        dr = torch.zeros((len(locs), xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+        items.append((dm, ds, locs, dr))
+        pairs.append(xg.Pair(d_master=dm.data_ptr(), m_nx=nx, m_ny=ny, d_slave=ds.data_ptr(), s_nx=nx, s_ny=ny,
+                             x_offset=0, y_offset=0, astretcha=0.0, locs=locs.ctypes.data, nlocs=len(locs),
+                             strip_len=nxl, xsearch=xs, ysearch=xs, d_results=dr.data_ptr()))
+        total += len(locs)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    stack = xg.Stack(xg.params(64, 64), device=dev.index)
+    stream = torch.cuda.Stream(dev)            # graph capture needs a stream of its own
+    with torch.cuda.stream(stream):
+        t1 = time.perf_counter()
+        stack.autotune(pairs, stream.cuda_stream)
+        torch.cuda.synchronize()
+        tune_s = time.perf_counter() - t1
+        stack.set_graph(True)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+        clocks = ClockSampler(dev.index)
+        clocks.start()
+        ms = _timed(lambda: stack.run(pairs, stream.cuda_stream), flush, stream, args.steps, args.warmup)
+        clk = clocks.stop()
+    st = stack.stats()
+    img_gb = sum(it[0].numel() * 2 * 2 for it in items) / 1e9
+    line = {"metric": "xcorr windows/s, stack of 32 pairs, mixed 64/128/256 windows", "value": args.steps * total / (ms / 1e3),
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "stack", "pairs": 32, "windows": total, "images_gb": img_gb,
+                       "window_mix": {str(2 * x): int(sum(p.nlocs for p in pairs if p.xsearch == x)) for x in (32, 64, 128)},
+                       "l2": "flushed between steps (256 MB write)", "generation_s": gen_s, "autotune_s": tune_s},
+            "stack_stats": {"launches_last_graph": int(st.last_graph_launches), "graph_replays": int(st.graph_replays),
+                            "buckets": int(st.buckets),
+                            "bucket_batch": [int(st.bucket_batch[i]) for i in range(st.buckets)]},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank, world, _ = _env_rank()
     if rank != 0:
@@ -415,6 +549,9 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="headline", choices=["headline", "frame", "stack"],
+                    help="headline: the 1000-window 128x128 case (default); frame: 40,000 windows of 256x256 on "
+                         "a 10240x30720 pair; stack: 32 pairs with mixed window sizes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the refined-path measurement")
     ap.add_argument("--no-precision-form", action="store_true", help="skip the tensor-core DFT measurement")
@@ -425,6 +562,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "frame":
+        run_frame(args)
+    elif args.workload == "stack":
+        run_stack(args)
     else:
         run_ours(args)
 

@@ -52,18 +52,19 @@ __global__ void k_tc_prepare(const float *__restrict__ A, int K, float scale, ui
 }
 
 template <int MT, int NT, int KC>
-__global__ void __launch_bounds__(128) k_tc_gemm_check(const uint8_t *__restrict__ a_prep, int K,
+__global__ void __launch_bounds__(256) k_tc_gemm_check(const uint8_t *__restrict__ a_prep, int K,
                                                         const float *__restrict__ B, int Ntot, float bscale,
                                                         float cscale, float *__restrict__ C, int *err) {
     const int n0 = blockIdx.x * NT;
-    auto loadB2 = [&](int k, int n) {
-        return make_float2(B[(size_t)k * Ntot + n0 + n] * bscale, B[(size_t)(k + 1) * Ntot + n0 + n] * bscale);
+    auto load = [&](int k, int n) {
+        return make_float2(B[(size_t)k * Ntot + n0 + n], B[(size_t)(k + 1) * Ntot + n0 + n]);
     };
+    auto cvt = [&](float2 v, int, int) { return make_float2(v.x * bscale, v.y * bscale); };
     auto epi = [&](int m, int c0, const float *v) {
 #pragma unroll
         for (int i = 0; i < 16; i++) C[(size_t)m * Ntot + n0 + c0 + i] = v[i] * cscale;
     };
-    tc::gemm_block<MT, NT, KC, false>(a_prep, K, loadB2, epi, err);
+    tc::gemm_block<MT, NT, KC, 256, false>(a_prep, K, load, cvt, epi, err);
 }
 
 template <int MT, int NT, int KC>
@@ -81,7 +82,7 @@ xcg_status run_check(int K, int Ntot, const float *A, const float *B, float *C, 
         e = cudaFuncSetAttribute(k_tc_gemm_check<MT, NT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
     }
     if (e == cudaSuccess) {
-        k_tc_gemm_check<MT, NT, KC><<<Ntot / NT, 128, G::SMEM, s>>>(prep, K, B, Ntot, 1.0f, 1.0f, C, err);
+        k_tc_gemm_check<MT, NT, KC><<<Ntot / NT, 256, G::SMEM, s>>>(prep, K, B, Ntot, 1.0f, 1.0f, C, err);
         e = cudaGetLastError();
     }
     int herr = 0;
@@ -103,52 +104,67 @@ __device__ __forceinline__ unsigned *ymax_slot(const Plan &P, int w) {
     return reinterpret_cast<unsigned *>(P.surf + (size_t)w * P.nyc * P.nxc);
 }
 
+constexpr int TC_THREADS = 256;
+
+// Epilogue transpose: the warp holds a 32 (lanes = rows m) x 16 (columns)
+// block; rows m = 2j + c are the re/im parts of 16 complex outputs j.  It is
+// passed through the (then idle) stage memory so that each store instruction
+// writes one output j's 16 complex values: out(j, col) receives c = 0/1 for
+// lane pairs, col = lane / 2.
+template <class Out>
+__device__ __forceinline__ void warp_store_t(const float *v, Out out) {
+    extern __shared__ __align__(1024) uint8_t tc_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *sc = reinterpret_cast<float *>(tc_smem) + warp * (32 * 17);
+#pragma unroll
+    for (int i = 0; i < 16; i++) sc[lane * 17 + i] = v[i];
+    __syncwarp();
+#pragma unroll 4
+    for (int j = 0; j < 16; j++) out(j, lane >> 1, lane & 1, sc[(2 * j + (lane & 1)) * 17 + (lane >> 1)]);
+    __syncwarp();
+}
+
 template <int N>
-__global__ void __launch_bounds__(128, 1) k_tc_rows(Plan P) {
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tc_rows(Plan P) {
     const int w = blockIdx.y, r0 = blockIdx.x * 128;
     float2 *z = P.zrow + (size_t)w * P.npy * N;
     if (blockIdx.x == 0 && threadIdx.x == 0) *ymax_slot(P, w) = 0u;
-    auto loadB2 = [&](int k, int n) {
-        const float2 v = z[(size_t)(r0 + n) * N + (k >> 1)];
-        return make_float2(v.x * S_ROW, v.y * S_ROW);
-    };
+    auto load = [&](int k, int n) { return z[(size_t)(r0 + n) * N + (k >> 1)]; };
+    auto cvt = [&](float2 v, int, int) { return make_float2(v.x * S_ROW, v.y * S_ROW); };
     auto epi = [&](int m, int n0, const float *v) {
         float *base = reinterpret_cast<float *>(z) + (m & 1);
         const int kx = m >> 1;
 #pragma unroll
         for (int i = 0; i < 16; i++) base[((size_t)(r0 + n0 + i) * N + kx) * 2] = v[i] * (1.0f / S_ROW);
     };
-    tc::gemm_block<2 * N / 128, 128, 32, true>(P.tc_a_row, 2 * N, loadB2, epi, P.tc_err);
+    tc::gemm_block<2 * N / 128, 128, 32, TC_THREADS, true>(P.tc_a_row, 2 * N, load, cvt, epi, P.tc_err);
 }
 
 template <int M>
-__global__ void __launch_bounds__(128, 1) k_tc_cols(Plan P) {
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tc_cols(Plan P) {
     const int N = P.npx;
     const int w = blockIdx.y, kx0 = blockIdx.x * 128;
     float2 *z = P.zrow + (size_t)w * M * N;
     float ymax = 0.f;
-    auto loadB2 = [&](int k, int n) {
-        const float2 v = z[(size_t)(k >> 1) * N + kx0 + n];
-        return make_float2(v.x * S_COL, v.y * S_COL);
-    };
+    auto load = [&](int k, int n) { return z[(size_t)(k >> 1) * N + kx0 + n]; };
+    auto cvt = [&](float2 v, int, int) { return make_float2(v.x * S_COL, v.y * S_COL); };
     auto epi = [&](int m, int n0, const float *v) {
-        float *base = reinterpret_cast<float *>(z) + (m & 1);
-        const int ky = m >> 1;
-#pragma unroll
-        for (int i = 0; i < 16; i++) {
-            const float o = v[i] * (1.0f / S_COL);
-            base[((size_t)ky * N + kx0 + n0 + i) * 2] = o;
+        const int ky0 = (m & ~31) >> 1;          // the warp's 16 rows ky0 .. ky0+15
+        float *zf = reinterpret_cast<float *>(z);
+        warp_store_t(v, [&](int j, int col, int c, float x) {
+            const float o = x * (1.0f / S_COL);
+            zf[((size_t)(ky0 + j) * N + kx0 + n0 + col) * 2 + c] = o;
             ymax = fmaxf(ymax, fabsf(o));
-        }
+        });
     };
-    tc::gemm_block<2 * M / 128, 128, 32, false>(P.tc_a_col, 2 * M, loadB2, epi, P.tc_err);
+    tc::gemm_block<2 * M / 128, 128, 32, TC_THREADS, false>(P.tc_a_col, 2 * M, load, cvt, epi, P.tc_err);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ymax = fmaxf(ymax, __shfl_xor_sync(0xffffffffu, ymax, o));
     if ((threadIdx.x & 31) == 0) atomicMax(ymax_slot(P, w), __float_as_uint(ymax));
 }
 
 template <int M>
-__global__ void __launch_bounds__(128, 1) k_tc_inv(Plan P) {
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tc_inv(Plan P) {
     const int N = P.npx;
     const int w = blockIdx.x;
     const float2 *z = P.zrow + (size_t)w * M * N;
@@ -180,11 +196,20 @@ __global__ void __launch_bounds__(128, 1) k_tc_inv(Plan P) {
     const float dc1 = (float)(msh[0] * (double)N * (double)M);
     const float m2 = (float)msh[1];
     const float su = ssh;
-    auto loadB2 = [&](int k, int n) {
+    auto load = [&](int k, int n) {
+        const int ky = k >> 1;
+        float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (n <= N / 2) {
+            const float2 z1 = z[(size_t)ky * N + n];
+            const float2 z2 = z[(size_t)((M - ky) & (M - 1)) * N + ((N - n) & (N - 1))];
+            r = make_float4(z1.x, z1.y, z2.x, z2.y);
+        }
+        return r;
+    };
+    auto cvt = [&](float4 r, int k, int n) {
         if (n > N / 2) return make_float2(0.f, 0.f);
         const int ky = k >> 1;
-        const float2 z1 = z[(size_t)ky * N + n];
-        const float2 z2 = z[(size_t)((M - ky) & (M - 1)) * N + ((N - n) & (N - 1))];
+        const float2 z1 = make_float2(r.x, r.y), z2 = make_float2(r.z, r.w);
         // A1 = (z1 + conj z2)/2, A2 = (z1 - conj z2)/(2i)
         float2 A1 = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
         float2 A2 = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
@@ -197,12 +222,13 @@ __global__ void __launch_bounds__(128, 1) k_tc_inv(Plan P) {
         return make_float2(pr.x * su, pr.y * su);
     };
     auto epi = [&](int m, int n0, const float *v) {
-        float *q = reinterpret_cast<float *>(P.qspec + ((size_t)w * P.nyc + (m >> 1)) * P.qpitch) + (m & 1);
-#pragma unroll
-        for (int i = 0; i < 16; i++)
-            if (n0 + i <= N / 2) q[2 * (n0 + i)] = v[i] / su;
+        const int yq0 = (m & ~31) >> 1;          // the warp's 16 surface rows
+        float *q = reinterpret_cast<float *>(P.qspec + (size_t)w * P.nyc * P.qpitch);
+        warp_store_t(v, [&](int j, int col, int c, float x) {
+            if (n0 + col <= N / 2) q[((size_t)(yq0 + j) * P.qpitch + n0 + col) * 2 + c] = x / su;
+        });
     };
-    tc::gemm_block<M / 128, 144, 32, false>(P.tc_a_inv, 2 * M, loadB2, epi, P.tc_err);
+    tc::gemm_block<M / 128, 144, 32, TC_THREADS, false>(P.tc_a_inv, 2 * M, load, cvt, epi, P.tc_err);
 }
 
 // Real 2x2-block embedding of rows [row0, row0 + nrows) of an n-point DFT
@@ -279,13 +305,13 @@ xcg_status tc_enable(xcg_ctx *c) {
 }
 
 void launch_tc_rows(const Plan &P, cudaStream_t s) {
-    k_tc_rows<256><<<dim3(P.npy / 128, P.nwin), 128, tc::GemmGeom<4, 128, 32>::SMEM, s>>>(P);
+    k_tc_rows<256><<<dim3(P.npy / 128, P.nwin), TC_THREADS, tc::GemmGeom<4, 128, 32>::SMEM, s>>>(P);
 }
 void launch_tc_cols(const Plan &P, cudaStream_t s) {
-    k_tc_cols<256><<<dim3(P.npx / 128, P.nwin), 128, tc::GemmGeom<4, 128, 32>::SMEM, s>>>(P);
+    k_tc_cols<256><<<dim3(P.npx / 128, P.nwin), TC_THREADS, tc::GemmGeom<4, 128, 32>::SMEM, s>>>(P);
 }
 void launch_tc_inv(const Plan &P, cudaStream_t s) {
-    k_tc_inv<256><<<P.nwin, 128, tc::GemmGeom<2, 144, 32>::SMEM, s>>>(P);
+    k_tc_inv<256><<<P.nwin, TC_THREADS, tc::GemmGeom<2, 144, 32>::SMEM, s>>>(P);
 }
 
 }  // namespace xcg

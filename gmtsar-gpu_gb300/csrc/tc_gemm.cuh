@@ -49,14 +49,21 @@ __host__ __device__ inline size_t prepared_bytes(int K) {
     return (size_t)(K / KC) * 2 * GemmGeom<MT, NT, KC>::A_TILE;
 }
 
-// Run the block.  loadB2(k, n) -> float2: B elements (k, n) and (k+1, n) of
-// this block (k even in [0, K), n in [0, NT)), already scaled into the FP16
-// range.  K_FAST: consecutive threads take consecutive k pairs (B stored with
-// k contiguous), else consecutive n.  epi(m, n0, v): the 16 accumulator
-// values of row m (m in [0, MT*128)), columns n0..n0+15.
-template <int MT, int NT, int KC, bool K_FAST, class LoadB2, class Epi>
-__device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, LoadB2 loadB2, Epi epi, int *err) {
+// Run the block with NTHR threads (128 or 256).  load(k, n) fetches the raw
+// data behind B elements (k, n) and (k+1, n) of this block (k even in [0, K),
+// n in [0, NT)); cvt(raw, k, n) -> float2 turns it into the two values,
+// already scaled into the FP16 range.  Each thread fetches its share of
+// chunk c+1 into registers before the MMAs of chunk c are issued, so global
+// latency overlaps the tensor work.  K_FAST: consecutive threads take
+// consecutive k pairs (B stored with k contiguous), else consecutive n.
+// epi(m, n0, v): the 16 accumulator values of row m (m in [0, MT*128)),
+// columns n0..n0+15.
+template <int MT, int NT, int KC, int NTHR, bool K_FAST, class Load, class Cvt, class Epi>
+__device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, Load load, Cvt cvt, Epi epi, int *err) {
     using G = GemmGeom<MT, NT, KC>;
+    static_assert(NTHR == 128 || NTHR == 256, "threads");
+    constexpr int PAIRS = NT * (KC / 2);
+    constexpr int ITEMS = (PAIRS + NTHR - 1) / NTHR;
     extern __shared__ __align__(1024) uint8_t tc_smem[];
     uint8_t *stage_base = tc_smem;
     uint64_t *bar_a = reinterpret_cast<uint64_t *>(tc_smem + 2 * (size_t)G::STAGE);   // [2]
@@ -82,6 +89,23 @@ __device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, LoadB2 loa
     const uint32_t tmem = *tmem_sh;
     constexpr uint32_t idesc = idesc_f16_f32(128, NT);
 
+    using Raw = decltype(load(0, 0));
+    Raw raw[ITEMS];
+    auto item = [&](int it, int &n, int &k2) {
+        const int i = tid + it * NTHR;
+        n = K_FAST ? i / (KC / 2) : i % NT;
+        k2 = K_FAST ? i % (KC / 2) : i / NT;
+        return i < PAIRS;
+    };
+    auto fetch = [&](int c) {
+#pragma unroll
+        for (int it = 0; it < ITEMS; it++) {
+            int n, k2;
+            if (item(it, n, k2)) raw[it] = load(c * KC + 2 * k2, n);
+        }
+    };
+    fetch(0);
+
     int issued = 0;                       // chunks whose MMAs were committed
     int copied = 0;                       // chunks whose A copy was started
     for (int c = 0; c < nchunks; c++) {
@@ -100,10 +124,11 @@ __device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, LoadB2 loa
         // (adjacent halves of one 16-byte core row), hi and lo tiles
         __half *bhi = reinterpret_cast<__half *>(st + 2 * G::A_TILE);
         __half *blo = reinterpret_cast<__half *>(st + 2 * G::A_TILE + G::B_TILE);
-        for (int i = tid; i < NT * (KC / 2); i += 128) {
-            const int n = K_FAST ? i / (KC / 2) : i % NT;
-            const int k2 = K_FAST ? i % (KC / 2) : i / NT;
-            const float2 v = loadB2(c * KC + 2 * k2, n);
+#pragma unroll
+        for (int it = 0; it < ITEMS; it++) {
+            int n, k2;
+            if (!item(it, n, k2)) continue;
+            const float2 v = cvt(raw[it], c * KC + 2 * k2, n);
             __half h0, l0, h1, l1;
             split_f16(v.x, h0, l0);
             split_f16(v.y, h1, l1);
@@ -111,6 +136,7 @@ __device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, LoadB2 loa
             *reinterpret_cast<__half2 *>(bhi + off) = __halves2half2(h0, h1);
             *reinterpret_cast<__half2 *>(blo + off) = __halves2half2(l0, l1);
         }
+        if (c + 1 < nchunks) fetch(c + 1);     // in flight while this chunk's MMAs are issued
         fence_async_smem();
         __syncthreads();
         if (tid == 0) {
@@ -151,13 +177,16 @@ __device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, LoadB2 loa
     if (copied > issued && tid == 0) (void)mbar_wait(&bar_a[(copied - 1) & 1], ((copied - 1) >> 1) & 1, kMaxPolls);
     fence_after_sync();
     if (ok && issued == nchunks) {
+        // warp w reads lanes 32*(w%4); with 8 warps the two halves take
+        // alternate 16-column groups
+        constexpr int WG = NTHR / 128;
 #pragma unroll 1
         for (int t = 0; t < MT; t++) {
 #pragma unroll 1
-            for (int n0 = 0; n0 < NT; n0 += 16) {
+            for (int n0 = 16 * (warp >> 2); n0 < NT; n0 += 16 * WG) {
                 float v[16];
-                tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(t * NT + n0), v);
-                epi(t * 128 + 32 * warp + lane, n0, v);
+                tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(t * NT + n0), v);
+                epi(t * 128 + 32 * (warp & 3) + lane, n0, v);
             }
         }
     } else if (tid == 0) {

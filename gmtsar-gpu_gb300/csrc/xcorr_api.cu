@@ -11,6 +11,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <complex>
 #include <string>
 #include <vector>
@@ -263,6 +264,8 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
             XCG_CK_C(cudaEventCreateWithFlags(&c->ev_join[k], cudaEventDisableTiming), "cudaEventCreate");
         }
         XCG_CK_C(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+        for (int k = 0; k < 2; k++)
+            XCG_CK_C(cudaStreamCreateWithFlags(&c->copy_stream[k], cudaStreamNonBlocking), "cudaStreamCreate");
     }
 #undef XCG_CK_C
     c->stats.scratch_bytes = c->scratch_bytes;
@@ -294,6 +297,9 @@ void xcg_destroy(xcg_ctx *c) {
         if (c->ev_join[k]) cudaEventDestroy(c->ev_join[k]);
     }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    for (int k = 0; k < 2; k++)
+        if (c->copy_stream[k]) { cudaStreamSynchronize(c->copy_stream[k]); cudaStreamDestroy(c->copy_stream[k]); }
+    for (cudaEvent_t ev : c->band_ready) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -321,12 +327,7 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     memset(&c->stats, 0, sizeof c->stats);
     c->stats.scratch_bytes = c->scratch_bytes;
     if (nlocs == 0) return XCG_OK;
-    int bw = c->max_batch;
-    // enough windows for two batches of >= 256: split so the two slots overlap
-    if (nlocs >= 512 && (nlocs + 1) / 2 < bw) bw = (nlocs + 1) / 2;
-    if (strip_len > 0 && strip_len <= bw) bw = ((bw + strip_len - 1) / strip_len) * strip_len;   // whole strips
-    if (bw > c->max_batch) bw = (c->max_batch / (strip_len > 0 ? strip_len : 1)) * (strip_len > 0 ? strip_len : 1);
-    if (bw < 1) bw = c->max_batch;
+    const int bw = xcg::ctx_batch_windows(c, nlocs, strip_len);
     xcg::Plan P = xcg::ctx_plan(c);
     P.single.master = d_master; P.single.m_nx = m_nx; P.single.m_ny = m_ny;
     P.single.slave = d_slave; P.single.s_nx = s_nx; P.single.s_ny = s_ny;
@@ -376,7 +377,18 @@ static Plan with_slot(Plan P, size_t off) {
     return P;
 }
 
-xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s) {
+int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len) {
+    int bw = c->max_batch;
+    // enough windows for two batches of >= 256: split so the two slots overlap
+    if (nlocs >= 512 && (nlocs + 1) / 2 < bw) bw = (nlocs + 1) / 2;
+    if (strip_len > 0 && strip_len <= bw) bw = ((bw + strip_len - 1) / strip_len) * strip_len;   // whole strips
+    if (bw > c->max_batch) bw = (c->max_batch / (strip_len > 0 ? strip_len : 1)) * (strip_len > 0 ? strip_len : 1);
+    if (bw < 1) bw = c->max_batch;
+    return bw;
+}
+
+xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s, const cudaEvent_t *ready,
+                      int nready) {
     // launch slots: rows, columns, peak, subpixel; the precision form splits
     // the column stage into three tensor-core DFT stages
     const bool tcf = P.tc_form != 0;
@@ -410,6 +422,7 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
         if (Q.nwin > maxw) maxw = Q.nwin;
         Q.locs = locs0 + Q.win0;
         Q.winref = ref0 ? ref0 + Q.win0 : nullptr;
+        for (int k = 0; k < nready; k++) XCG_CK(cudaStreamWaitEvent(ss, ready[(size_t)b * nready + k], 0), "cudaStreamWaitEvent");
         for (int k = 0; k < nk; k++) {
             if (c->profiling) cudaEventRecord(c->events[ei++], ss);
             const bool tm = Q.corr_mode < 2;     // -time / -time4: full-search surface
@@ -491,11 +504,62 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
         c->io_cap = nlocs;
     }
     cudaStream_t s = c->stream;
-    XCG_CK(cudaMemcpyAsync(c->d_img[0], master, need[0], cudaMemcpyHostToDevice, s), "copy master");
-    XCG_CK(cudaMemcpyAsync(c->d_img[1], slave, need[1], cudaMemcpyHostToDevice, s), "copy slave");
     XCG_CK(cudaMemcpyAsync(c->d_locs, locs, (size_t)nlocs * sizeof(xcg_loc), cudaMemcpyHostToDevice, s), "copy locs");
-    xcg_status st = xcg_correlate_device(c, c->d_img[0], m_nx, m_ny, c->d_img[1], s_nx, s_ny, x_offset, y_offset,
-                                         astretcha, c->d_locs, nlocs, strip_len, c->d_res, (void *)s);
+    // Copy the images in row bands, master and slave on their own streams:
+    // batch b waits only for the rows its windows read (master rows up to
+    // y + npy/2, slave rows up to y + y_offset + ishft + npy/2), so the copy of
+    // later rows overlaps the first batches' kernels.
+    const int bw = xcg::ctx_batch_windows(c, nlocs, strip_len);
+    const int nb = (nlocs + bw - 1) / bw;
+    while (c->band_ready.size() < (size_t)nb * 2) {
+        cudaEvent_t ev;
+        XCG_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+        c->band_ready.push_back(ev);
+    }
+    XCG_CK(cudaEventRecord(c->ev_fork, s), "cudaEventRecord");     // after whatever the caller queued on s
+    for (int k = 0; k < 2; k++) XCG_CK(cudaStreamWaitEvent(c->copy_stream[k], c->ev_fork, 0), "cudaStreamWaitEvent");
+    const int npy = c->base.npy;
+    const int ny[2] = {m_ny, s_ny};
+    const size_t rowb[2] = {(size_t)m_nx * es, (size_t)s_nx * es};
+    const void *src[2] = {master, slave};
+    int done[2] = {0, 0};
+    std::vector<int> starts;
+    for (int b = 0; b < nb; b++) {
+        const int w0 = b * bw, w1 = (b + 1 == nb) ? nlocs : (b + 1) * bw;
+        starts.push_back(w0);
+        int want[2] = {0, 0};
+        for (int w = w0; w < w1; w++) {
+            const int y = locs[w].y, ishft = (int)((double)y * astretcha);
+            want[0] = std::max(want[0], y + npy / 2 + 1);
+            want[1] = std::max(want[1], y + y_offset + ishft + npy / 2 + 1);
+        }
+        if (b + 1 == nb) { want[0] = ny[0]; want[1] = ny[1]; }
+        for (int k = 0; k < 2; k++) {
+            const int to = std::min(std::max(want[k], done[k]), ny[k]);
+            if (to > done[k])
+                XCG_CK(cudaMemcpyAsync((char *)c->d_img[k] + (size_t)done[k] * rowb[k], (const char *)src[k] + (size_t)done[k] * rowb[k],
+                                       (size_t)(to - done[k]) * rowb[k], cudaMemcpyHostToDevice, c->copy_stream[k]),
+                       k ? "copy slave" : "copy master");
+            done[k] = to;
+            XCG_CK(cudaEventRecord(c->band_ready[(size_t)b * 2 + k], c->copy_stream[k]), "cudaEventRecord");
+        }
+    }
+    starts.push_back(nlocs);
+    XCG_CK(cudaSetDevice(c->device), "cudaSetDevice");
+    memset(&c->stats, 0, sizeof c->stats);
+    c->stats.scratch_bytes = c->scratch_bytes;
+    xcg::Plan P = xcg::ctx_plan(c);
+    P.single.master = c->d_img[0]; P.single.m_nx = m_nx; P.single.m_ny = m_ny;
+    P.single.slave = c->d_img[1]; P.single.s_nx = s_nx; P.single.s_ny = s_ny;
+    P.single.x_offset = x_offset; P.single.y_offset = y_offset; P.single.astretcha = astretcha;
+    P.single.strip_len = strip_len;
+    P.single.nlocs = nlocs;
+    P.single.out = c->d_res;
+    P.single.feat = c->features;
+    P.pairs = nullptr;
+    P.winref = nullptr;
+    P.locs = c->d_locs;
+    xcg_status st = xcg::ctx_launch(c, P, starts.data(), nb, s, c->band_ready.data(), 2);
     if (st != XCG_OK) return st;
     XCG_CK(cudaMemcpyAsync(results, c->d_res, (size_t)nlocs * sizeof(xcg_result), cudaMemcpyDeviceToHost, s), "copy results");
     XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");

@@ -23,6 +23,10 @@ struct xcg_ctx {
     int nslots = 2;
     cudaStream_t slot_stream[2] = {nullptr, nullptr};
     cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+    // host entry: the two images are copied on their own streams in row bands,
+    // one band per batch, and each batch waits only for its band
+    cudaStream_t copy_stream[2] = {nullptr, nullptr};
+    std::vector<cudaEvent_t> band_ready;      // [batch][2]
     size_t off_zrow, off_amp1, off_amp2c, off_part, off_oob, off_minmax, off_means, off_qspec, off_surf, off_md,
         off_mdnext, off_corr0n;
     // host-entry buffers
@@ -53,7 +57,11 @@ namespace xcg {
 Plan ctx_plan(const xcg_ctx *c);
 // Launch the four kernels for windows [starts[b], starts[b+1]) of the
 // window arrays in P (locs, winref), b < nbatch; updates the context stats.
-xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nbatch, cudaStream_t s);
+// ready (optional): nready events per batch that batch b waits for first.
+xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nbatch, cudaStream_t s,
+                      const cudaEvent_t *ready = nullptr, int nready = 0);
+// Windows per batch xcg_correlate_device uses for nlocs windows.
+int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len);
 void set_last_error(const char *msg);
 // precision form (tc_dft.cu)
 xcg_status tc_enable(xcg_ctx *c);

@@ -26,6 +26,11 @@
 #ifndef XCG_COLS_BLOCKS
 #define XCG_COLS_BLOCKS 5
 #endif
+// k_peak: one CTA per window, so the grid is about one wave; 4 resident CTAs
+// per SM (64 registers, a few spills) beat 3 for transforms up to 256 points
+#ifndef XCG_PEAK_BLOCKS
+#define XCG_PEAK_BLOCKS 4
+#endif
 
 namespace xcg {
 
@@ -111,7 +116,7 @@ __device__ __forceinline__ int slave_row_shift(const PairDev &pd, int y) {
 // sum is the only chunk-sum state kept in shared memory.  Rows live in
 // registers in the team layout (lane l: samples l + T*m); the next row's
 // samples are loaded while the current one is transformed.
-template <int N>
+template <int N, int LG>
 __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_rows(Plan P) {
     constexpr int T = fft_lanes(N);
     constexpr int TPW = 32 / T;
@@ -149,7 +154,10 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     const int sx0 = loc.x + pd.x_offset - N / 2;
     const int sy0 = loc.y + pd.y_offset + slave_row_shift(pd, loc.y) - npy / 2;
     bool oob = false;
-    const int ri = P.ri, lg = P.log2ri;
+    constexpr int ri = 1 << LG;
+    // kept fine samples k = ri*q + p - N/2 in [0, N) are q in [N/(2ri), 3N/(2ri)):
+    // with q = lane + T*m that is m in [KM0, KM1) for every lane and phase
+    constexpr int KM0 = (LG == 0) ? 0 : PER / (2 * ri), KM1 = (LG == 0) ? PER : 3 * PER / (2 * ri);
     float mn1 = INFINITY, mx1 = -INFINITY, mn2 = INFINITY, mx2 = -INFINITY;
 
     // raw samples of one patch row, team layout; 32-bit words (int16 pair or float)
@@ -162,11 +170,16 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         const int x0 = pt ? sx0 : mx0, y = (pt ? sy0 : my0) + r;
         const bool rowok = (y >= 0 && y < ny);
         const uint32_t *row = reinterpret_cast<const uint32_t *>(img) + (size_t)(rowok ? y : 0) * (size_t)nx;
+        if (rowok && x0 >= 0 && x0 + N <= nx) {          // the usual case: the whole row segment is inside
 #pragma unroll
-        for (int m = 0; m < PER; m++) {
-            const int x = x0 + lane + T * m;
-            if (rowok && x >= 0 && x < nx) raw[m] = __ldg(row + x);
-            else { raw[m] = 0u; oob = true; }
+            for (int m = 0; m < PER; m++) raw[m] = __ldg(row + x0 + lane + T * m);
+        } else {
+#pragma unroll
+            for (int m = 0; m < PER; m++) {
+                const int x = x0 + lane + T * m;
+                if (rowok && x >= 0 && x < nx) raw[m] = __ldg(row + x);
+                else { raw[m] = 0u; oob = true; }
+            }
         }
     };
     auto to_complex = [&](const uint32_t *raw, float2 *v) {
@@ -186,7 +199,7 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         float *row = rb + pt * N;
         float2 v[PER];
         to_complex(raw, v);
-        if (ri == 1) {
+        if (LG == 0) {
 #pragma unroll
             for (int m = 0; m < PER; m++) row[lane + T * m] = hypotf(v[m].x, v[m].y);
             return;
@@ -195,9 +208,9 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         // anyway, so their amplitudes use the cheaper sqrt(x^2 + y^2); hypotf is
         // kept where the samples are the input itself (ri == 1, bit-exact)
 #pragma unroll
-        for (int m = 0; m < PER; m++) {          // phase-0 samples are the input
-            const int k = ((lane + T * m) << lg) - N / 2;
-            if (k >= 0 && k < N) row[k] = sqrtf(fmaf(v[m].x, v[m].x, v[m].y * v[m].y));
+        for (int m = KM0; m < KM1; m++) {        // phase-0 samples are the input
+            const int k = ((lane + T * m) << LG) - N / 2;
+            row[k] = sqrtf(fmaf(v[m].x, v[m].x, v[m].y * v[m].y));
         }
 #pragma unroll 1
         for (int p = 1; p < ri; p++) {
@@ -212,9 +225,9 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
             for (int m = 0; m < PER; m++) v[m] = cmulf(v[m], __ldg(ph + lane + T * m));
             team_fft_reg<N, +1>(v, ex, tw, lane);
 #pragma unroll
-            for (int m = 0; m < PER; m++) {
-                const int k = ((lane + T * m) << lg) + p - N / 2;
-                if (k >= 0 && k < N) row[k] = sqrtf(fmaf(v[m].x, v[m].x, v[m].y * v[m].y));
+            for (int m = KM0; m < KM1; m++) {
+                const int k = ((lane + T * m) << LG) + p - N / 2;
+                row[k] = sqrtf(fmaf(v[m].x, v[m].x, v[m].y * v[m].y));
             }
         }
     };
@@ -241,16 +254,20 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         float *a2g = P.amp2c + ((size_t)w * P.ny_corr + (r - P.ysearch)) * P.nx_corr;
         float *acc1 = acc + tm * N, *acc2 = acc + ACC + tm * N;
         float2 v[PER];
+        // the slave mask's columns [xsearch, N - xsearch) (xsearch = N/4) and
+        // the time-correlation window's [xsearch, xsearch + nx_corr) are both
+        // m in [PER/4, 3 PER/4) for every lane
 #pragma unroll
         for (int m = 0; m < PER; m++) {
             const int e = lane + T * m;
             const float a1 = rb[e], a2 = rb[N + e];
-            const bool in = rin && (e >= P.xsearch) && (e < N - P.xsearch);
+            const bool cin = (m >= PER / 4) && (m < 3 * PER / 4);
+            const bool in = rin && cin;
             v[m] = make_float2(a1, in ? a2 : 0.f);
             mn1 = fminf(mn1, a1); mx1 = fmaxf(mx1, a1);
             if (in) { mn2 = fminf(mn2, a2); mx2 = fmaxf(mx2, a2); }
             a1g[e] = a1;
-            if (r2c && e >= P.xsearch && e < P.xsearch + P.nx_corr) a2g[e - P.xsearch] = a2;
+            if (r2c && cin) a2g[e - N / 4] = a2;
             // first reduction level in the reference's order: x[t] + x[t+512],
             // rows ir = 0 and 1 of this team
             if (ir == 0) { acc1[e] = a1; acc2[e] = a2; }
@@ -442,7 +459,7 @@ __global__ void __launch_bounds__(128, ColsGeom<M>::BLOCKS) k_cols(Plan P) {
 // the time correlation d_calc_time_corr_strip (do_time_int_xcorr.cu:71-100),
 // d_scaled_strip (conv_ampl_demean.cu:50-68) and d_cppow_strip (:75-95).
 template <int N>
-__global__ void __launch_bounds__(256) k_peak(Plan P) {
+__global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 ? 2 : 1)) k_peak(Plan P) {
     constexpr int T = fft_lanes(N);
     constexpr int PADN = fft_padded_len(N);
     constexpr int TWL = fft_twiddle_len(N);
@@ -668,18 +685,37 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
         tr[t] = s;
     }
     __syncthreads();
-    // column pass, real part only, and the argmax
+    // column pass, real part only, and the argmax: a thread keeps one column X
+    // of the row-pass result in registers (n2y = 8 values) and walks the
+    // output rows Y, four at a time; a warp shares Y, so the KY reads broadcast
     unsigned long long best = 0ull;
-    for (int e = threadIdx.x; e < ny2 * nx2; e += blockDim.x) {
-        const int Y = e / nx2, X = e - Y * nx2;
-        float re = 0.f;
-        for (int r = 0; r < n2y; r++) {
-            const float2 k = kys[Y * n2y + r], t = tr[r * nx2 + X];
-            re = fmaf(k.x, t.x, re);
-            re = fmaf(-k.y, t.y, re);
+    const int tpr = nx2 < (int)blockDim.x ? nx2 : (int)blockDim.x;     // threads per output row
+    const int rp = (int)blockDim.x / tpr;                               // rows in flight per pass
+    for (int X = threadIdx.x % tpr; X < nx2; X += tpr) {
+        float2 tc[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) tc[r] = tr[r * nx2 + X];
+        for (int Y = threadIdx.x / tpr; Y < ny2; Y += 4 * rp) {
+            float re[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int yy = Y + j * rp;
+                if (yy >= ny2) break;
+#pragma unroll
+                for (int r = 0; r < 8; r++) {
+                    const float2 k = kys[yy * 8 + r];
+                    re[j] = fmaf(k.x, tc[r].x, re[j]);
+                    re[j] = fmaf(-k.y, tc[r].y, re[j]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int yy = Y + j * rp;
+                if (yy >= ny2) break;
+                const unsigned long long kk = argmax_key(re[j], (unsigned)(yy * nx2 + X));
+                best = kk > best ? kk : best;
+            }
         }
-        const unsigned long long kk = argmax_key(re, (unsigned)e);
-        best = kk > best ? kk : best;
     }
     best = warp_max_u64(best);
     const int warp = threadIdx.x >> 5;
@@ -772,7 +808,12 @@ static size_t subpix_smem(const Plan &P) {
 
 template <int N>
 static cudaError_t setup_rows() {
-    return cudaFuncSetAttribute(k_rows<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>());
+    cudaError_t e = cudaSuccess;
+    auto set = [&](auto kern) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rows_smem<N>());
+    };
+    set(k_rows<N, 0>); set(k_rows<N, 1>); set(k_rows<N, 2>); set(k_rows<N, 3>);
+    return e;
 }
 template <int M>
 static cudaError_t setup_cols(int) {
@@ -812,7 +853,12 @@ cudaError_t kernels_setup(const Plan &P) {
 template <int N>
 static void launch_rows_t(const Plan &P, cudaStream_t s) {
     dim3 grid(P.nchunks / 4, P.nwin);          // one chunk per warp, 4 warps per CTA
-    k_rows<N><<<grid, 128, rows_smem<N>(), s>>>(P);
+    switch (P.log2ri) {                        // range interpolation factor 1, 2, 4, 8
+        case 0: k_rows<N, 0><<<grid, 128, rows_smem<N>(), s>>>(P); break;
+        case 1: k_rows<N, 1><<<grid, 128, rows_smem<N>(), s>>>(P); break;
+        case 2: k_rows<N, 2><<<grid, 128, rows_smem<N>(), s>>>(P); break;
+        default: k_rows<N, 3><<<grid, 128, rows_smem<N>(), s>>>(P); break;
+    }
 }
 template <int M>
 static void launch_cols_t(const Plan &P, cudaStream_t s) {
