@@ -20,6 +20,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "team_fft.cuh"
 #include "xcorr_kernels.cuh"
 
@@ -182,15 +184,17 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
             }
         }
     };
+    const bool iq16 = (P.format == 0);
     auto to_complex = [&](const uint32_t *raw, float2 *v) {
+        if (iq16) {
 #pragma unroll
-        for (int m = 0; m < PER; m++) {
-            if (P.format == 0) {
+            for (int m = 0; m < PER; m++) {
                 const short lo = (short)(raw[m] & 0xffffu), hi = (short)(raw[m] >> 16);
                 v[m] = make_float2((float)lo, (float)hi);
-            } else {
-                v[m] = make_float2(__uint_as_float(raw[m]), 0.f);
             }
+        } else {
+#pragma unroll
+            for (int m = 0; m < PER; m++) v[m] = make_float2(__uint_as_float(raw[m]), 0.f);
         }
     };
 
@@ -256,23 +260,26 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         float2 v[PER];
         // the slave mask's columns [xsearch, N - xsearch) (xsearch = N/4) and
         // the time-correlation window's [xsearch, xsearch + nx_corr) are both
-        // m in [PER/4, 3 PER/4) for every lane
+        // m in [PER/4, 3 PER/4) for every lane.  First reduction level in the
+        // reference's order, x[t] + x[t+512]: rows ir = 0 and 1 of this team.
+        auto packed = [&](auto first) {
 #pragma unroll
-        for (int m = 0; m < PER; m++) {
-            const int e = lane + T * m;
-            const float a1 = rb[e], a2 = rb[N + e];
-            const bool cin = (m >= PER / 4) && (m < 3 * PER / 4);
-            const bool in = rin && cin;
-            v[m] = make_float2(a1, in ? a2 : 0.f);
-            mn1 = fminf(mn1, a1); mx1 = fmaxf(mx1, a1);
-            if (in) { mn2 = fminf(mn2, a2); mx2 = fmaxf(mx2, a2); }
-            a1g[e] = a1;
-            if (r2c && cin) a2g[e - N / 4] = a2;
-            // first reduction level in the reference's order: x[t] + x[t+512],
-            // rows ir = 0 and 1 of this team
-            if (ir == 0) { acc1[e] = a1; acc2[e] = a2; }
-            else { acc1[e] = acc1[e] + a1; acc2[e] = acc2[e] + a2; }
-        }
+            for (int m = 0; m < PER; m++) {
+                const int e = lane + T * m;
+                const float a1 = rb[e], a2 = rb[N + e];
+                const bool cin = (m >= PER / 4) && (m < 3 * PER / 4);
+                const bool in = rin && cin;
+                v[m] = make_float2(a1, in ? a2 : 0.f);
+                mn1 = fminf(mn1, a1); mx1 = fmaxf(mx1, a1);
+                if (in) { mn2 = fminf(mn2, a2); mx2 = fmaxf(mx2, a2); }
+                a1g[e] = a1;
+                if (r2c && cin) a2g[e - N / 4] = a2;
+                if constexpr (decltype(first)::value) { acc1[e] = a1; acc2[e] = a2; }
+                else { acc1[e] = acc1[e] + a1; acc2[e] = acc2[e] + a2; }
+            }
+        };
+        if (ir == 0) packed(std::true_type{});
+        else packed(std::false_type{});
         // the precision form transforms the packed rows on the tensor cores
         if (!P.tc_form) team_fft_reg<N, -1>(v, ex, tw, lane);
         float2 *zg = P.zrow + ((size_t)w * npy + r) * N;

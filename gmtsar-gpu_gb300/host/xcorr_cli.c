@@ -309,8 +309,13 @@ int main(int argc, char **argv)
 
     struct timespec t0, t1;
     clock_gettime(CLOCK_MONOTONIC, &t0);
+    /* scratch for this job's batches only: two batches of whole strips (the
+     * library's default holds 2048 windows per slot) */
+    int max_batch = xc.nlocs >= 512 ? (xc.nlocs + 1) / 2 : xc.nlocs;
+    if (xc.nxl > 0) max_batch = ((max_batch + xc.nxl - 1) / xc.nxl) * xc.nxl;
+    if (max_batch > 2048 || max_batch < 1) max_batch = 0;
     xcg_ctx *ctx = NULL;
-    xcg_status st = xcg_create(&p, 0, 0, &ctx);
+    xcg_status st = xcg_create(&p, 0, max_batch, &ctx);
     if (st != XCG_OK) {
         fprintf(stderr, "xcorr: %s: %s\n", xcg_status_string(st), xcg_last_error());
         return 1;
