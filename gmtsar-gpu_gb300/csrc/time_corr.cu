@@ -212,6 +212,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tcorr(Plan P) {
 __global__ void __launch_bounds__(TC_THREADS) k_tpeak(Plan P) {
     __shared__ double rd[8];
     __shared__ int ri_[8];
+    __shared__ int oob_sh;
     __shared__ double bc[2];
     const int w = blockIdx.x;
     const int nxc = P.nxc, nyc = P.nyc, ns = nxc * nyc;
@@ -234,6 +235,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_tpeak(Plan P) {
     const double vstar = bc[0];
     const float F = (float)vstar;
     const bool down = (double)F < vstar;
+    if (warp == 0) {          // any chunk that read outside an image, reduced by one warp
+        int f = 0;
+        for (int i = l32; i < P.nchunks; i += 32) f |= P.oobmap[(size_t)w * P.nchunks + i];
+        f = __any_sync(0xffffffffu, f != 0);
+        if (l32 == 0) oob_sh = f;
+    }
     int pick = down ? -1 : ns;
     for (int k = threadIdx.x; k < ns; k += TC_THREADS) {
         const double v = at(k);
@@ -265,9 +272,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tpeak(Plan P) {
         o.yoff = -1 * ipeak;
         o.corr = F;
         o.ip = ip; o.jp = jp;
-        int fl = 0;
-        for (int i = 0; i < P.nchunks; i++) fl |= P.oobmap[(size_t)w * P.nchunks + i] ? XCG_FLAG_OOB : 0;
-        o.flags = fl;
+        o.flags = oob_sh ? XCG_FLAG_OOB : 0;
         o.cmax = vstar;
         o.cave = 0.0;
         o.cave_true = 0.0;

@@ -25,6 +25,9 @@
 #include "team_fft.cuh"
 #include "xcorr_kernels.cuh"
 
+#ifndef XCG_COLS_THREADS
+#define XCG_COLS_THREADS 128
+#endif
 #ifndef XCG_COLS_BLOCKS
 #define XCG_COLS_BLOCKS 5
 #endif
@@ -335,13 +338,14 @@ struct ColsGeom {
     static constexpr int T = fft_lanes(M);
     static constexpr int PADM = fft_padded_len(M);
     static constexpr int CS = PADM + 1;
-    static constexpr int CP = 128 / T;            // column pairs per CTA = teams
+    static constexpr int THREADS = XCG_COLS_THREADS;
+    static constexpr int CP = THREADS / T;        // column pairs per CTA = teams
     static constexpr int TWL = fft_twiddle_len(M);
-    static constexpr int BLOCKS = (M >= 1024) ? 2 : (M >= 512 ? 3 : XCG_COLS_BLOCKS);
+    static constexpr int BLOCKS = (M >= 1024) ? 2 * 128 / THREADS : (M >= 512 ? 3 * 128 / THREADS : XCG_COLS_BLOCKS);
 };
 
 template <int M>
-__global__ void __launch_bounds__(128, ColsGeom<M>::BLOCKS) k_cols(Plan P) {
+__global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_cols(Plan P) {
     using G = ColsGeom<M>;
     constexpr int T = G::T, CS = G::CS, CP = G::CP, TWL = G::TWL;
     constexpr int PER = M / T;
@@ -359,8 +363,8 @@ __global__ void __launch_bounds__(128, ColsGeom<M>::BLOCKS) k_cols(Plan P) {
     const int team = warp * (32 / T) + l32 / T;
 
     for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_col[i];
-    {   // thread t stages slot t % (2CP) for rows t / (2CP) + k * 128/(2CP): all loads first
-        constexpr int RSTEP = 128 / (2 * CP);
+    {   // thread t stages slot t % (2CP) for rows t / (2CP) + k * THREADS/(2CP): all loads first
+        constexpr int RSTEP = G::THREADS / (2 * CP);
         constexpr int NLD = M / RSTEP;
         const int s = threadIdx.x % (2 * CP), row0 = threadIdx.x / (2 * CP);
         int col;
@@ -494,17 +498,30 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
     // The reference's surface is exactly zero when either demeaned patch is
     // (its FFTs of zeros stay zeros); the packed transform here would leave
     // rounding residue of the other patch, so that case is set explicitly.
-    if (threadIdx.x == 0) {
+    if (warp == 0) {          // per-chunk extremes and out-of-image flags, reduced by one warp
         const float *mm = P.minmax + (size_t)w * 4 * P.nchunks;
         float a = INFINITY, b = -INFINITY, c2 = INFINITY, d = -INFINITY;
-        for (int i = 0; i < P.nchunks; i++) {
+        int oobf = 0;
+        for (int i = l32; i < P.nchunks; i += 32) {
             a = fminf(a, mm[i]); b = fmaxf(b, mm[P.nchunks + i]);
             c2 = fminf(c2, mm[2 * P.nchunks + i]); d = fmaxf(d, mm[3 * P.nchunks + i]);
+            oobf |= P.oobmap[(size_t)w * P.nchunks + i];
         }
-        const float m1f = (float)P.means[2 * w], m2f = (float)P.means[2 * w + 1];
-        const bool z1 = (a == b) && (a - m1f == 0.f);
-        const bool z2 = (c2 == d) && (c2 - m2f == 0.f);
-        bc[2] = (z1 || z2) ? 0.0 : 1.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a = fminf(a, __shfl_xor_sync(0xffffffffu, a, o));
+            b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+            c2 = fminf(c2, __shfl_xor_sync(0xffffffffu, c2, o));
+            d = fmaxf(d, __shfl_xor_sync(0xffffffffu, d, o));
+        }
+        oobf = __any_sync(0xffffffffu, oobf != 0);
+        if (l32 == 0) {
+            const float m1f = (float)P.means[2 * w], m2f = (float)P.means[2 * w + 1];
+            const bool z1 = (a == b) && (a - m1f == 0.f);
+            const bool z2 = (c2 == d) && (c2 - m2f == 0.f);
+            bc[2] = (z1 || z2) ? 0.0 : 1.0;
+            bc[3] = oobf ? 1.0 : 0.0;
+        }
     }
     __syncthreads();
     const float keep = (float)bc[2];
@@ -564,8 +581,9 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
     const float *a1 = P.amp1 + (size_t)w * M * N + (size_t)(P.ysearch + (int)ipeak) * N + (int)jpeak + P.xsearch;
     const float *a2 = P.amp2c + (size_t)w * P.ny_corr * P.nx_corr;
     long long sn = 0, s1 = 0, s2 = 0;
-    for (int i = threadIdx.x; i < P.ny_corr * P.nx_corr; i += NT) {
-        const int r = i / P.nx_corr, cc = i - r * P.nx_corr;
+    constexpr int NXC = N / 2;          // nx_corr = 2 xsearch = npx / 2
+    for (int i = threadIdx.x; i < P.ny_corr * NXC; i += NT) {
+        const int r = i / NXC, cc = i - r * NXC;
         float va = a1[(size_t)r * N + cc] - m1f;
         va = va * 1.0f;
         float vb = a2[i] - m2f;
@@ -593,9 +611,7 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
         o.yoff = -1 * ipeak;
         o.corr = (float)gamma;
         o.ip = ip; o.jp = jp;
-        int fl = 0;
-        for (int i = 0; i < P.nchunks; i++) fl |= P.oobmap[(size_t)w * P.nchunks + i] ? XCG_FLAG_OOB : 0;
-        o.flags = fl;
+        o.flags = (bc[3] != 0.0) ? XCG_FLAG_OOB : 0;
         o.cmax = cmax;
         o.cave = rd[0] / (double)(nxc * nyc);
         o.cave_true = rd[8] / (double)(nxc * nyc);
@@ -871,7 +887,7 @@ template <int M>
 static void launch_cols_t(const Plan &P, cudaStream_t s) {
     constexpr int CP = ColsGeom<M>::CP;
     dim3 grid((P.npx / 2) / CP, P.nwin);
-    k_cols<M><<<grid, 128, cols_smem<M>(P.nchunks), s>>>(P);
+    k_cols<M><<<grid, ColsGeom<M>::THREADS, cols_smem<M>(P.nchunks), s>>>(P);
 }
 template <int N>
 static void launch_peak_t(const Plan &P, cudaStream_t s) {
