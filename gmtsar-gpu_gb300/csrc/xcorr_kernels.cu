@@ -322,6 +322,15 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     }
 }
 
+// ---------------------------------------------------------------- cp.async
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory"); }
+
 // ---------------------------------------------------------------- k_cols
 // Replaces the column half of the forward FFTs, d_mulaconjb/d_Cmul
 // (do_freq_xcorr.cu:32-64,106-109), the inverse FFT's column half and
@@ -363,23 +372,28 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
     const int team = warp * (32 / T) + l32 / T;
 
     for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_col[i];
-    {   // thread t stages slot t % (2CP) for rows t / (2CP) + k * THREADS/(2CP): all loads first
-        constexpr int RSTEP = G::THREADS / (2 * CP);
+    {   // thread t stages column slot t % CP of both halves (partner slots CP.., then
+        // own slots 0..) for rows t / CP + k * THREADS/CP, as two cp.async groups:
+        // the partner columns land first and are transformed while the own
+        // columns are still arriving
+        constexpr int RSTEP = G::THREADS / CP;
         constexpr int NLD = M / RSTEP;
-        const int s = threadIdx.x % (2 * CP), row0 = threadIdx.x / (2 * CP);
-        int col;
-        if (s < CP) col = kx0 + s;
-        else { const int kx = kx0 + s - CP; col = (kx == 0) ? N / 2 : N - kx; }
-        const float2 *src = P.zrow + (size_t)w * M * N + col;
-        constexpr int BATCH = (NLD < 16) ? NLD : 16;
-#pragma unroll 1
-        for (int k0 = 0; k0 < NLD; k0 += BATCH) {
-            float2 t[BATCH];
-#pragma unroll
-            for (int k = 0; k < BATCH; k++) t[k] = __ldg(src + (size_t)(row0 + (k0 + k) * RSTEP) * N);
-#pragma unroll
-            for (int k = 0; k < BATCH; k++) cols[s * CS + fft_pad(row0 + (k0 + k) * RSTEP)] = t[k];
+        const int sl = threadIdx.x % CP, row0 = threadIdx.x / CP;
+        const int kxp = kx0 + sl;
+        const int pcol = (kxp == 0) ? N / 2 : N - kxp;
+        const float2 *base = P.zrow + (size_t)w * M * N;
+#pragma unroll 8
+        for (int k = 0; k < NLD; k++) {
+            const int r = row0 + k * RSTEP;
+            cp_async8(cols + (CP + sl) * CS + fft_pad(r), base + (size_t)r * N + pcol);
         }
+        cp_async_commit();
+#pragma unroll 8
+        for (int k = 0; k < NLD; k++) {
+            const int r = row0 + k * RSTEP;
+            cp_async8(cols + sl * CS + fft_pad(r), base + (size_t)r * N + kxp);
+        }
+        cp_async_commit();
     }
     if (warp == 0) {
         // patch means (:719-724): the reference adds the FP32 chunk sums in
@@ -398,7 +412,8 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
             if (b == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
         }
     }
-    __syncthreads();
+    cp_async_wait<1>();                          // partner columns in (this thread's copies)
+    __syncthreads();                             // ... and everyone's
     const float dc1 = (float)(sh[0] * (double)N * (double)M);
     const float m2 = (float)sh[1];
 
@@ -413,6 +428,8 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
     team_fft_reg<M, -1>(z, pa, tw, lane);
 #pragma unroll
     for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
+    cp_async_wait<0>();                          // own columns in
+    __syncthreads();
 #pragma unroll
     for (int m = 0; m < PER; m++) z[m] = a[fft_pad(lane + T * m)];
     __syncwarp();
