@@ -197,7 +197,14 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *
         P.locs = d_locs + w0;
         P.skip = nullptr;
         xcg::launch_rows(P, s);
-        xcg::launch_cols(P, s);
+        if (P.tc_form) {                         // precision form: tensor-core DFT stages
+            xcg::launch_tc_rows(P, s);
+            xcg::launch_tc_cols(P, s);
+            xcg::launch_tc_inv(P, s);
+            c->stats.launches += 2;
+        } else {
+            xcg::launch_cols(P, s);
+        }
         xcg::launch_peak(P, s);
         xcg::ref_launch_infer(r->R, c->ref_feat + (size_t)w0 * 81, c->ref_pred + (size_t)w0 * 3, P.nwin, s);
         xcg::launch_decide(P, c->ref_pred + (size_t)w0 * 3, c->ref_skip + w0, max_sigma, max_disagree, s);

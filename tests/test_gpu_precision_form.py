@@ -62,3 +62,37 @@ def test_precision_form_error_against_fp64(cfg1):
     print("rms offset error vs FP64 oracle [range, azimuth] px:", out)
     assert out["split_fp16_tc"][0] <= out["fp32"][0] + 0.01
     assert out["split_fp16_tc"][1] <= out["fp32"][1] + 0.01
+
+
+def test_refined_path_in_precision_form(cfg1):
+    """The refined path runs the tensor-core stages too and agrees with its
+    FP32 form (the refiner sees the same neighbourhoods to ~1e-6)."""
+    import os
+    torch = pytest.importorskip("torch")
+    from xcorr_gb300 import refiner_train as rt
+    wpath = os.path.join(os.path.dirname(xg.__file__), "..", "..", "refiner", "subpix_refiner.f32")
+    if not os.path.exists(wpath):
+        pytest.skip("no trained refiner weights")
+    g, m, s, locs, d, r32, rtc, _ = cfg1
+    dev = torch.device("cuda")
+    dm, ds = torch.from_numpy(m).to(dev), torch.from_numpy(s).to(dev)
+    dl = torch.from_numpy(locs).to(dev)
+    out = []
+    ref = xg.Refiner(0, max_batch=64)
+    ref.set_params(rt.load_weights(wpath))
+    with xg.Context(xg.params(64, 64)) as ctx:
+        for form in (0, 1):
+            ctx.set_dft_form(form)
+            dr = torch.zeros((len(locs), xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+            ctx.correlate_device_refined(ref, dm.data_ptr(), m.shape[1], m.shape[0], ds.data_ptr(), s.shape[1],
+                                         s.shape[0], dl.data_ptr(), len(locs), dr.data_ptr(), strip_len=d["nxl"],
+                                         max_sigma=0.15)
+            torch.cuda.synchronize()
+            out.append(np.frombuffer(dr.cpu().numpy().tobytes(), dtype=xg.RESULT_DTYPE))
+    ref.close()
+    a, b = out
+    np.testing.assert_array_equal(a["ip"], b["ip"])
+    np.testing.assert_array_equal(a["jp"], b["jp"])
+    assert np.mean(a["flags"] == b["flags"]) > 0.99
+    both = ((a["flags"] & xg.FLAG_REFINED) != 0) & ((b["flags"] & xg.FLAG_REFINED) != 0)
+    assert np.max(np.abs(a["xfrac"][both] - b["xfrac"][both])) < 1e-3
