@@ -163,6 +163,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_cols(Plan P) {
     if ((threadIdx.x & 31) == 0) atomicMax(ymax_slot(P, w), __float_as_uint(ymax));
 }
 
+// shapes of the three stages for square n x n transforms (n = 128 or 256)
+template <int n>
+struct TcShapes {
+    static constexpr int MT_FWD = 2 * n / 128;                   // 128-row tiles of the 2n real outputs
+    static constexpr int MT_INV = n / 128;                       // 2 nyc = n real outputs of the band
+    static constexpr int NT_INV = ((n / 2 + 1 + 15) / 16) * 16;  // kx in [0, n/2], padded to 16
+};
+
 template <int M>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_inv(Plan P) {
     const int N = P.npx;
@@ -228,7 +236,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_inv(Plan P) {
             if (n0 + col <= N / 2) q[((size_t)(yq0 + j) * P.qpitch + n0 + col) * 2 + c] = x / su;
         });
     };
-    tc::gemm_block<M / 128, 144, 32, TC_THREADS, false>(P.tc_a_inv, 2 * M, load, cvt, epi, P.tc_err);
+    tc::gemm_block<TcShapes<M>::MT_INV, TcShapes<M>::NT_INV, 32, TC_THREADS, false>(P.tc_a_inv, 2 * M, load, cvt, epi,
+                                                                                  P.tc_err);
 }
 
 // Real 2x2-block embedding of rows [row0, row0 + nrows) of an n-point DFT
@@ -250,43 +259,37 @@ std::vector<float> dft_blocks(int n, int row0, int nrows, int sign) {
 
 }  // namespace
 
-// Prepares the three DFT operands for a 256 x 256 geometry and switches the
-// context's plan to the precision form.
-xcg_status tc_enable(xcg_ctx *c) {
+// Prepares the three DFT operands for an n x n geometry (n = 128, 256) and
+// switches the context's plan to the precision form.
+template <int n>
+static xcg_status tc_enable_t(xcg_ctx *c) {
+    using S = TcShapes<n>;
     Plan &B = c->base;
-    if (B.npx != 256 || B.npy != 256) {
-        set_last_error("the precision form needs 128 x 128 windows (256 x 256 transforms)");
-        return XCG_ERR_UNSUPPORTED;
-    }
-    if (B.corr_mode != 2) {
-        set_last_error("the precision form applies to the frequency-domain mode");
-        return XCG_ERR_UNSUPPORTED;
-    }
-    if (B.tc_a_row) { B.tc_form = 1; return XCG_OK; }
-    const int N = B.npx, M = B.npy;
-    const std::vector<float> ar = dft_blocks(N, 0, N, -1), ac = dft_blocks(M, 0, M, -1),
-                             ai = dft_blocks(M, B.ysearch, B.nyc, +1);
-    const size_t br = tc::prepared_bytes<4, 128, 32>(2 * N), bc = tc::prepared_bytes<4, 128, 32>(2 * M),
-                 bi = tc::prepared_bytes<2, 144, 32>(2 * M);
+    const std::vector<float> ar = dft_blocks(n, 0, n, -1), ai = dft_blocks(n, B.ysearch, B.nyc, +1);
+    const size_t br = tc::prepared_bytes<S::MT_FWD, 128, 32>(2 * n), bi = tc::prepared_bytes<S::MT_INV, S::NT_INV, 32>(2 * n);
     uint8_t *prep = nullptr;
     float *tmp = nullptr;
     int *err = nullptr;
-    cudaError_t e = cudaMalloc(&prep, br + bc + bi);
+    cudaError_t e = cudaMalloc(&prep, 2 * br + bi);
     if (e == cudaSuccess) e = cudaMalloc(&tmp, ar.size() * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
+    // rows and columns use the same forward operand (square transforms)
     if (e == cudaSuccess) e = cudaMemcpy(tmp, ar.data(), ar.size() * sizeof(float), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) { k_tc_prepare<4, 128, 32><<<256, 256>>>(tmp, 2 * N, 1.0f, prep); e = cudaDeviceSynchronize(); }
-    if (e == cudaSuccess) e = cudaMemcpy(tmp, ac.data(), ac.size() * sizeof(float), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) { k_tc_prepare<4, 128, 32><<<256, 256>>>(tmp, 2 * M, 1.0f, prep + br); e = cudaDeviceSynchronize(); }
+    if (e == cudaSuccess) { k_tc_prepare<S::MT_FWD, 128, 32><<<256, 256>>>(tmp, 2 * n, 1.0f, prep); e = cudaDeviceSynchronize(); }
+    if (e == cudaSuccess) e = cudaMemcpy(prep + br, prep, br, cudaMemcpyDeviceToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(tmp, ai.data(), ai.size() * sizeof(float), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) { k_tc_prepare<2, 144, 32><<<256, 256>>>(tmp, 2 * M, 1.0f, prep + br + bc); e = cudaDeviceSynchronize(); }
+    if (e == cudaSuccess) {
+        k_tc_prepare<S::MT_INV, S::NT_INV, 32><<<256, 256>>>(tmp, 2 * n, 1.0f, prep + 2 * br);
+        e = cudaDeviceSynchronize();
+    }
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_tc_rows<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<4, 128, 32>::SMEM);
+        e = cudaFuncSetAttribute(k_tc_rows<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<S::MT_FWD, 128, 32>::SMEM);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_tc_cols<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<4, 128, 32>::SMEM);
+        e = cudaFuncSetAttribute(k_tc_cols<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<S::MT_FWD, 128, 32>::SMEM);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_tc_inv<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<2, 144, 32>::SMEM);
+        e = cudaFuncSetAttribute(k_tc_inv<n>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::GemmGeom<S::MT_INV, S::NT_INV, 32>::SMEM);
     cudaFree(tmp);
     if (e != cudaSuccess) {
         cudaFree(prep);
@@ -298,21 +301,39 @@ xcg_status tc_enable(xcg_ctx *c) {
     c->tc_err = err;
     B.tc_a_row = prep;
     B.tc_a_col = prep + br;
-    B.tc_a_inv = prep + br + bc;
+    B.tc_a_inv = prep + 2 * br;
     B.tc_err = err;
     B.tc_form = 1;
     return XCG_OK;
 }
 
-void launch_tc_rows(const Plan &P, cudaStream_t s) {
-    k_tc_rows<256><<<dim3(P.npy / 128, P.nwin), TC_THREADS, tc::GemmGeom<4, 128, 32>::SMEM, s>>>(P);
+xcg_status tc_enable(xcg_ctx *c) {
+    Plan &B = c->base;
+    if (B.npx != B.npy || (B.npx != 256 && B.npx != 128)) {
+        set_last_error("the precision form needs square windows of 64 or 128 (128- or 256-point transforms)");
+        return XCG_ERR_UNSUPPORTED;
+    }
+    if (B.corr_mode != 2) {
+        set_last_error("the precision form applies to the frequency-domain mode");
+        return XCG_ERR_UNSUPPORTED;
+    }
+    if (B.tc_a_row) { B.tc_form = 1; return XCG_OK; }
+    return B.npx == 256 ? tc_enable_t<256>(c) : tc_enable_t<128>(c);
 }
-void launch_tc_cols(const Plan &P, cudaStream_t s) {
-    k_tc_cols<256><<<dim3(P.npx / 128, P.nwin), TC_THREADS, tc::GemmGeom<4, 128, 32>::SMEM, s>>>(P);
+
+template <int n>
+static void launch_tc_t(const Plan &P, int stage, cudaStream_t s) {
+    using S = TcShapes<n>;
+    if (stage == 0)
+        k_tc_rows<n><<<dim3(n / 128, P.nwin), TC_THREADS, tc::GemmGeom<S::MT_FWD, 128, 32>::SMEM, s>>>(P);
+    else if (stage == 1)
+        k_tc_cols<n><<<dim3(n / 128, P.nwin), TC_THREADS, tc::GemmGeom<S::MT_FWD, 128, 32>::SMEM, s>>>(P);
+    else
+        k_tc_inv<n><<<P.nwin, TC_THREADS, tc::GemmGeom<S::MT_INV, S::NT_INV, 32>::SMEM, s>>>(P);
 }
-void launch_tc_inv(const Plan &P, cudaStream_t s) {
-    k_tc_inv<256><<<P.nwin, TC_THREADS, tc::GemmGeom<2, 144, 32>::SMEM, s>>>(P);
-}
+void launch_tc_rows(const Plan &P, cudaStream_t s) { P.npx == 256 ? launch_tc_t<256>(P, 0, s) : launch_tc_t<128>(P, 0, s); }
+void launch_tc_cols(const Plan &P, cudaStream_t s) { P.npx == 256 ? launch_tc_t<256>(P, 1, s) : launch_tc_t<128>(P, 1, s); }
+void launch_tc_inv(const Plan &P, cudaStream_t s) { P.npx == 256 ? launch_tc_t<256>(P, 2, s) : launch_tc_t<128>(P, 2, s); }
 
 }  // namespace xcg
 

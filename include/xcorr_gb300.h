@@ -270,7 +270,8 @@ xcg_status xcg_fit_offsets(const xcg_result *d_results, const xcg_loc *d_locs, i
  * correlation and the inverse column DFT of the product run as split-FP16
  * (hi + lo) tensor-core matmuls with FP32 accumulation (tcgen05), the range
  * interpolation and the inverse row transform staying FP32.  Form 1 needs
- * 128 x 128 windows (xsearch = ysearch = 64, 256 x 256 transforms). */
+ * square windows of 64 or 128 (xsearch = ysearch = 32 or 64: 128- or
+ * 256-point transforms); other shapes return XCG_ERR_UNSUPPORTED. */
 xcg_status xcg_set_dft_form(xcg_ctx *ctx, int32_t form);
 
 /* Diagnostic: the split-FP16 tensor-core GEMM engine of the precision form

@@ -15,6 +15,7 @@ import pytest
 
 import build as pkg_build
 import golden_util as gu
+import xcorr_gb300 as xg
 from cases import CASES, PRF
 from xcorr_gb300 import synth
 
@@ -54,3 +55,24 @@ def test_program_matches_reference_lines(program, tmp_path, name, whole):
     assert np.max(np.abs(a[:, 4] - b[:, 4])) <= 0.0100001
     same = sum(x == y for x, y in zip(lines, g["lines"]))
     assert same >= len(lines) - max(1, len(lines) // 200)
+
+
+@pytest.mark.parametrize("flag,fname,mode", [("-time", "time_xcorr.dat", 0), ("-time4", "time_xcorr_Gatelli.dat", 1)])
+def test_program_time_modes(program, tmp_path, flag, fname, mode):
+    """-time / -time4 write their own file (xcorr.cu:467-469) with the lines
+    the library's full-search mode gives for the same windows."""
+    case = CASES["xs32"]
+    g = gu.load("xs32")
+    synth.write_case(str(tmp_path), case["spec"], 0, 0, PRF, None)
+    p = subprocess.run([program, "master.PRM", "aligned.PRM", flag] + case["flags"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    assert "time cross correlation" in p.stderr
+    lines = open(tmp_path / fname).read().splitlines()
+    m, s, locs, d, xoff, yoff, ast = gu.case_inputs("xs32", g)
+    pr = xg.params(d["xsearch"], d["ysearch"], d["ri"], d["interp_flag"], d["ifc"], corr_mode=mode)
+    with xg.Context(pr) as ctx:
+        r = ctx.correlate(m, s, locs, xoff, yoff, ast, strip_len=d["nxl"])
+    xo_, yo_ = xg.output_offsets(r, d["ri"], xoff, yoff, locs[:, 1], ast)
+    want = [" %d %6.3f %d %6.3f %6.2f " % (locs[i, 0], xo_[i], locs[i, 1], yo_[i], r["corr"][i]) for i in range(len(locs))]
+    assert lines == want
