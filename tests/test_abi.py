@@ -32,8 +32,9 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layouts_match_header(tmp_path):
     c = tmp_path / "sz.c"
     c.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "xcorr_gb300.h"\n'
-                 'int main(void){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(xcg_params), sizeof(xcg_loc),'
-                 ' sizeof(xcg_result), offsetof(xcg_result, cmax), offsetof(xcg_result, corr0n), sizeof(xcg_stats));'
+                 'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(xcg_params), sizeof(xcg_loc),'
+                 ' sizeof(xcg_result), offsetof(xcg_result, cmax), offsetof(xcg_result, corr0n), sizeof(xcg_stats),'
+                 ' sizeof(xcg_pair), sizeof(xcg_stack_stats), sizeof(xcg_fit), offsetof(xcg_fit, azimuth));'
                  'return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I" + os.path.dirname(HEADER), str(c), "-o", str(exe)], check=True)
@@ -45,11 +46,15 @@ def test_struct_layouts_match_header(tmp_path):
     assert vals[3] == xg.RESULT_DTYPE.fields["cmax"][1]
     assert vals[4] == xg.RESULT_DTYPE.fields["corr0n"][1]
     assert vals[5] == ctypes.sizeof(xg.Stats)
+    assert vals[6] == ctypes.sizeof(xg.Pair)
+    assert vals[7] == ctypes.sizeof(xg.StackStats)
+    assert vals[8] == ctypes.sizeof(xg.Fit)
+    assert vals[9] == xg.Fit.azimuth.offset
 
 
 def test_create_rejects_bad_parameters_without_touching_the_gpu():
     # argument validation happens before any device call
-    for kw in (dict(xsearch=48), dict(xsearch=16), dict(ri=3), dict(interp_factor=12)):
+    for kw in (dict(xsearch=48), dict(xsearch=16), dict(ri=3), dict(interp_factor=12), dict(corr_mode=3)):
         p = xg.params(**kw)
         with pytest.raises(xg.XcgError) as e:
             xg.Context(p)
