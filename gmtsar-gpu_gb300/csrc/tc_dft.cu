@@ -64,12 +64,13 @@ __global__ void __launch_bounds__(256) k_tc_gemm_check(const uint8_t *__restrict
 #pragma unroll
         for (int i = 0; i < 16; i++) C[(size_t)m * Ntot + n0 + c0 + i] = v[i] * cscale;
     };
-    tc::gemm_block<MT, NT, KC, 256, false>(a_prep, K, load, cvt, epi, err);
+    tc::gemm_block_ws<MT, NT, 4, false>(a_prep, K, load, cvt, epi, err);
 }
 
 template <int MT, int NT, int KC>
 xcg_status run_check(int K, int Ntot, const float *A, const float *B, float *C, cudaStream_t s) {
-    using G = tc::GemmGeom<MT, NT, KC>;
+    using G = tc::WsGeom<MT, NT, 4>;
+    static_assert(KC == G::KC, "chunk width");
     if (K % KC || Ntot % NT) return XCG_ERR_ARG;
     uint8_t *prep = nullptr;
     int *err = nullptr;
@@ -105,6 +106,12 @@ __device__ __forceinline__ unsigned *ymax_slot(const Plan &P, int w) {
 }
 
 constexpr int TC_THREADS = 256;
+// forward stages (512 accumulator columns): 16-wide K chunks, 4 stages (160 KB);
+// the inverse (up to 288 columns, fewer MMAs per chunk): 32-wide chunks, 4 stages
+constexpr int TC_STAGES = 4;
+constexpr int TC_KC = 16;
+constexpr int TC_STAGES_INV = 4;
+constexpr int TC_KC_INV = 32;
 
 // Epilogue transpose: the warp holds a 32 (lanes = rows m) x 16 (columns)
 // block; rows m = 2j + c are the re/im parts of 16 complex outputs j.  It is
@@ -137,7 +144,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_rows(Plan P) {
 #pragma unroll
         for (int i = 0; i < 16; i++) base[((size_t)(r0 + n0 + i) * N + kx) * 2] = v[i] * (1.0f / S_ROW);
     };
-    tc::gemm_block<2 * N / 128, 128, 32, TC_THREADS, true>(P.tc_a_row, 2 * N, load, cvt, epi, P.tc_err);
+    tc::gemm_block_ws<2 * N / 128, 128, TC_STAGES, true>(P.tc_a_row, 2 * N, load, cvt, epi, P.tc_err);
 }
 
 template <int M>
@@ -157,7 +164,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_cols(Plan P) {
             ymax = fmaxf(ymax, fabsf(o));
         });
     };
-    tc::gemm_block<2 * M / 128, 128, 32, TC_THREADS, false>(P.tc_a_col, 2 * M, load, cvt, epi, P.tc_err);
+    tc::gemm_block_ws<2 * M / 128, 128, TC_STAGES, false>(P.tc_a_col, 2 * M, load, cvt, epi, P.tc_err);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ymax = fmaxf(ymax, __shfl_xor_sync(0xffffffffu, ymax, o));
     if ((threadIdx.x & 31) == 0) atomicMax(ymax_slot(P, w), __float_as_uint(ymax));
@@ -236,8 +243,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_inv(Plan P) {
             if (n0 + col <= N / 2) q[((size_t)(yq0 + j) * P.qpitch + n0 + col) * 2 + c] = x / su;
         });
     };
-    tc::gemm_block<TcShapes<M>::MT_INV, TcShapes<M>::NT_INV, 32, TC_THREADS, false>(P.tc_a_inv, 2 * M, load, cvt, epi,
-                                                                                  P.tc_err);
+    tc::gemm_block_ws<TcShapes<M>::MT_INV, TcShapes<M>::NT_INV, TC_STAGES_INV, false, TC_KC_INV>(P.tc_a_inv, 2 * M, load,
+                                                                                                cvt, epi, P.tc_err);
 }
 
 // Real 2x2-block embedding of rows [row0, row0 + nrows) of an n-point DFT
@@ -266,7 +273,8 @@ static xcg_status tc_enable_t(xcg_ctx *c) {
     using S = TcShapes<n>;
     Plan &B = c->base;
     const std::vector<float> ar = dft_blocks(n, 0, n, -1), ai = dft_blocks(n, B.ysearch, B.nyc, +1);
-    const size_t br = tc::prepared_bytes<S::MT_FWD, 128, 32>(2 * n), bi = tc::prepared_bytes<S::MT_INV, S::NT_INV, 32>(2 * n);
+    const size_t br = tc::ws_prepared_bytes<S::MT_FWD, 128, TC_STAGES>(2 * n),
+                 bi = tc::ws_prepared_bytes<S::MT_INV, S::NT_INV, TC_STAGES_INV, TC_KC_INV>(2 * n);
     uint8_t *prep = nullptr;
     float *tmp = nullptr;
     int *err = nullptr;
@@ -276,20 +284,22 @@ static xcg_status tc_enable_t(xcg_ctx *c) {
     if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
     // rows and columns use the same forward operand (square transforms)
     if (e == cudaSuccess) e = cudaMemcpy(tmp, ar.data(), ar.size() * sizeof(float), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) { k_tc_prepare<S::MT_FWD, 128, 32><<<256, 256>>>(tmp, 2 * n, 1.0f, prep); e = cudaDeviceSynchronize(); }
+    if (e == cudaSuccess) { k_tc_prepare<S::MT_FWD, 128, TC_KC><<<256, 256>>>(tmp, 2 * n, 1.0f, prep); e = cudaDeviceSynchronize(); }
     if (e == cudaSuccess) e = cudaMemcpy(prep + br, prep, br, cudaMemcpyDeviceToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(tmp, ai.data(), ai.size() * sizeof(float), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        k_tc_prepare<S::MT_INV, S::NT_INV, 32><<<256, 256>>>(tmp, 2 * n, 1.0f, prep + 2 * br);
+        k_tc_prepare<S::MT_INV, S::NT_INV, TC_KC_INV><<<256, 256>>>(tmp, 2 * n, 1.0f, prep + 2 * br);
         e = cudaDeviceSynchronize();
     }
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_tc_rows<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<S::MT_FWD, 128, 32>::SMEM);
+        e = cudaFuncSetAttribute(k_tc_rows<n>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::WsGeom<S::MT_FWD, 128, TC_STAGES>::SMEM);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_tc_cols<n>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::GemmGeom<S::MT_FWD, 128, 32>::SMEM);
+        e = cudaFuncSetAttribute(k_tc_cols<n>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::WsGeom<S::MT_FWD, 128, TC_STAGES>::SMEM);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_tc_inv<n>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::GemmGeom<S::MT_INV, S::NT_INV, 32>::SMEM);
+                                 (int)tc::WsGeom<S::MT_INV, S::NT_INV, TC_STAGES_INV, TC_KC_INV>::SMEM);
     cudaFree(tmp);
     if (e != cudaSuccess) {
         cudaFree(prep);
@@ -325,11 +335,11 @@ template <int n>
 static void launch_tc_t(const Plan &P, int stage, cudaStream_t s) {
     using S = TcShapes<n>;
     if (stage == 0)
-        k_tc_rows<n><<<dim3(n / 128, P.nwin), TC_THREADS, tc::GemmGeom<S::MT_FWD, 128, 32>::SMEM, s>>>(P);
+        k_tc_rows<n><<<dim3(n / 128, P.nwin), TC_THREADS, tc::WsGeom<S::MT_FWD, 128, TC_STAGES>::SMEM, s>>>(P);
     else if (stage == 1)
-        k_tc_cols<n><<<dim3(n / 128, P.nwin), TC_THREADS, tc::GemmGeom<S::MT_FWD, 128, 32>::SMEM, s>>>(P);
+        k_tc_cols<n><<<dim3(n / 128, P.nwin), TC_THREADS, tc::WsGeom<S::MT_FWD, 128, TC_STAGES>::SMEM, s>>>(P);
     else
-        k_tc_inv<n><<<P.nwin, TC_THREADS, tc::GemmGeom<S::MT_INV, S::NT_INV, 32>::SMEM, s>>>(P);
+        k_tc_inv<n><<<P.nwin, TC_THREADS, tc::WsGeom<S::MT_INV, S::NT_INV, TC_STAGES_INV, TC_KC_INV>::SMEM, s>>>(P);
 }
 void launch_tc_rows(const Plan &P, cudaStream_t s) { P.npx == 256 ? launch_tc_t<256>(P, 0, s) : launch_tc_t<128>(P, 0, s); }
 void launch_tc_cols(const Plan &P, cudaStream_t s) { P.npx == 256 ? launch_tc_t<256>(P, 1, s) : launch_tc_t<128>(P, 1, s); }
@@ -348,9 +358,9 @@ extern "C" xcg_status xcg_tc_gemm_check(int32_t m_tiles, int32_t n_tile, int32_t
                                         const float *d_a, const float *d_b, float *d_c, void *stream) {
     if (!d_a || !d_b || !d_c || k <= 0 || n_total <= 0) return XCG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    if (m_tiles == 4 && n_tile == 128) return xcg::run_check<4, 128, 32>(k, n_total, d_a, d_b, d_c, s);
-    if (m_tiles == 2 && n_tile == 144) return xcg::run_check<2, 144, 32>(k, n_total, d_a, d_b, d_c, s);
-    if (m_tiles == 1 && n_tile == 256) return xcg::run_check<1, 256, 32>(k, n_total, d_a, d_b, d_c, s);
+    if (m_tiles == 4 && n_tile == 128) return xcg::run_check<4, 128, 16>(k, n_total, d_a, d_b, d_c, s);
+    if (m_tiles == 2 && n_tile == 144) return xcg::run_check<2, 144, 16>(k, n_total, d_a, d_b, d_c, s);
+    if (m_tiles == 1 && n_tile == 256) return xcg::run_check<1, 256, 16>(k, n_total, d_a, d_b, d_c, s);
     xcg::set_last_error("xcg_tc_gemm_check: shapes (4,128), (2,144), (1,256) only");
     return XCG_ERR_UNSUPPORTED;
 }

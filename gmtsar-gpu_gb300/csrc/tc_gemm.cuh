@@ -4,18 +4,17 @@
 // accumulated in FP32 in tensor memory (about 22 significant bits per
 // operand; the Alo Blo term is below FP32 rounding).
 //
-// One CTA of 128 threads computes an (MT*128) x NT block over the whole K:
+// One CTA of 256 threads computes an (MT*128) x NT block over the whole K:
 //  * A is a constant matrix prepared once in global memory in the exact
 //    shared-memory layout of each K chunk (hi tile then lo tile), so a single
 //    1-D bulk copy (TMA) per chunk stages it;
-//  * B is produced by the caller's functor (data, split on the fly) and
-//    written by all threads into the K-major core-matrix layout;
-//  * two stages: while the tensor core works on chunk c, the threads stage
-//    chunk c+1; stage reuse waits on the MMA commit of chunk c-1;
+//  * B is produced by the caller's functors (data, split on the fly) and
+//    written into the K-major core-matrix layout by six producer warps;
+//  * one lane issues the MMAs, tcgen05.commit releases each stage;
 //  * the accumulator (MT tiles of 128 lanes x NT columns) is read back with
-//    tcgen05.ld by the four warps and handed to the caller's epilogue.
-// Every mbarrier wait is bounded; on a timeout the kernel raises *err, waits
-// (bounded) for its own work in flight, frees tensor memory and returns.
+//    tcgen05.ld by the eight warps and handed to the caller's epilogue.
+// Every mbarrier wait is bounded; on a timeout the kernel raises *err and
+// every role winds down before tensor memory is freed.
 #pragma once
 #include <cuda_fp16.h>
 #include <stdint.h>
@@ -49,27 +48,46 @@ __host__ __device__ inline size_t prepared_bytes(int K) {
     return (size_t)(K / KC) * 2 * GemmGeom<MT, NT, KC>::A_TILE;
 }
 
-// Run the block with NTHR threads (128 or 256).  load(k, n) fetches the raw
-// data behind B elements (k, n) and (k+1, n) of this block (k even in [0, K),
-// n in [0, NT)); cvt(raw, k, n) -> float2 turns it into the two values,
-// already scaled into the FP16 range.  Each thread fetches its share of
-// chunk c+1 into registers before the MMAs of chunk c are issued, so global
-// latency overlaps the tensor work.  K_FAST: consecutive threads take
-// consecutive k pairs (B stored with k contiguous), else consecutive n.
-// epi(m, n0, v): the 16 accumulator values of row m (m in [0, MT*128)),
-// columns n0..n0+15.
-template <int MT, int NT, int KC, int NTHR, bool K_FAST, class Load, class Cvt, class Epi>
-__device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, Load load, Cvt cvt, Epi epi, int *err) {
-    using G = GemmGeom<MT, NT, KC>;
-    static_assert(NTHR == 128 || NTHR == 256, "threads");
+// ---------------------------------------------------------------------------
+// The block engine: NS stages of one KC-wide K chunk each, filled ahead of
+// the tensor core through full/empty mbarrier pairs (no CTA-wide barriers in
+// the main loop).
+//   warp 0, lane 0: issues the MMAs of chunk c once full[c % NS] has
+//     completed, then commits them to empty[c % NS];
+//   warp 1, lane 0: bulk-copies A chunk c into its stage (transaction count on
+//     full[c % NS]) once the stage is empty;
+//   warps 2..7: keep B chunks c+1 and c+2 loading into registers while chunk
+//     c is split and stored, fence for the async proxy and arrive on
+//     full[c % NS] (one arrival per warp).
+// With NS = 4 the producers run up to four chunks ahead of the MMAs.  All
+// waits are bounded; a timeout raises *err and every role winds down.
+template <int MT, int NT, int NS, int KC_ = 16>
+struct WsGeom {
+    static constexpr int KC = KC_;
+    static constexpr uint32_t SBO = KC * 16u;
+    static constexpr uint32_t A_TILE = (uint32_t)MT * 128u * KC * 2u;
+    static constexpr uint32_t B_TILE = (uint32_t)NT * KC * 2u;
+    static constexpr uint32_t STAGE = 2u * A_TILE + 2u * B_TILE;
+    static constexpr uint32_t TMEM_COLS_USED = (uint32_t)MT * NT;
+    static constexpr uint32_t TMEM_COLS = TMEM_COLS_USED <= 32 ? 32 : TMEM_COLS_USED <= 64 ? 64
+                                        : TMEM_COLS_USED <= 128 ? 128 : TMEM_COLS_USED <= 256 ? 256 : 512;
+    static_assert(TMEM_COLS_USED <= 512 && NT % 16 == 0 && NT <= 256, "shape");
+    static constexpr int PRODUCERS = 192;            // warps 2..7
+    static constexpr size_t SMEM = (size_t)NS * STAGE + (2 * NS + 1) * 8 + 16;
+};
+
+template <int MT, int NT, int NS, bool K_FAST, int KC_ = 16, class Load, class Cvt, class Epi>
+__device__ void gemm_block_ws(const uint8_t *__restrict__ a_prep, int K, Load load, Cvt cvt, Epi epi, int *err) {
+    using G = WsGeom<MT, NT, NS, KC_>;
+    constexpr int KC = G::KC;
     constexpr int PAIRS = NT * (KC / 2);
-    constexpr int ITEMS = (PAIRS + NTHR - 1) / NTHR;
+    constexpr int ITEMS = (PAIRS + G::PRODUCERS - 1) / G::PRODUCERS;
     extern __shared__ __align__(1024) uint8_t tc_smem[];
-    uint8_t *stage_base = tc_smem;
-    uint64_t *bar_a = reinterpret_cast<uint64_t *>(tc_smem + 2 * (size_t)G::STAGE);   // [2]
-    uint64_t *bar_mma = bar_a + 2;                                                    // [2]
-    uint32_t *tmem_sh = reinterpret_cast<uint32_t *>(bar_mma + 2);
-    int *abort_sh = reinterpret_cast<int *>(tmem_sh + 1);
+    uint64_t *full = reinterpret_cast<uint64_t *>(tc_smem + (size_t)NS * G::STAGE);
+    uint64_t *empty = full + NS;
+    uint64_t *done = empty + NS;
+    uint32_t *tmem_sh = reinterpret_cast<uint32_t *>(done + 1);
+    volatile int *abort_sh = reinterpret_cast<volatile int *>(tmem_sh + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nchunks = K / KC;
 
@@ -77,9 +95,9 @@ __device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, Load load,
         tmem_alloc(tmem_sh, G::TMEM_COLS);
         tmem_relinquish();
     }
-    if (tid == 0) {
-        mbar_init(&bar_a[0], 1); mbar_init(&bar_a[1], 1);
-        mbar_init(&bar_mma[0], 1); mbar_init(&bar_mma[1], 1);
+    if (tid == 32) {
+        for (int i = 0; i < NS; i++) { mbar_init(&full[i], G::PRODUCERS / 32 + 1); mbar_init(&empty[i], 1); }
+        mbar_init(done, 1);
         *abort_sh = 0;
         mbar_fence_init();
     }
@@ -89,101 +107,122 @@ __device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, Load load,
     const uint32_t tmem = *tmem_sh;
     constexpr uint32_t idesc = idesc_f16_f32(128, NT);
 
-    using Raw = decltype(load(0, 0));
-    Raw raw[ITEMS];
-    auto item = [&](int it, int &n, int &k2) {
-        const int i = tid + it * NTHR;
-        n = K_FAST ? i / (KC / 2) : i % NT;
-        k2 = K_FAST ? i % (KC / 2) : i / NT;
-        return i < PAIRS;
-    };
-    auto fetch = [&](int c) {
-#pragma unroll
-        for (int it = 0; it < ITEMS; it++) {
-            int n, k2;
-            if (item(it, n, k2)) raw[it] = load(c * KC + 2 * k2, n);
-        }
-    };
-    fetch(0);
-
-    int issued = 0;                       // chunks whose MMAs were committed
-    int copied = 0;                       // chunks whose A copy was started
-    for (int c = 0; c < nchunks; c++) {
-        const int s = c & 1;
-        uint8_t *st = stage_base + (size_t)s * G::STAGE;
-        // stage s was last read by the MMAs of chunk c-2
-        if (c >= 2 && !mbar_wait(&bar_mma[s], ((c - 2) >> 1) & 1, kMaxPolls)) *abort_sh = 1;
-        __syncthreads();
-        if (*abort_sh) break;
-        if (tid == 0) {
-            mbar_expect_tx(&bar_a[s], 2 * G::A_TILE);
-            bulk_g2s(st, a_prep + (size_t)c * 2 * G::A_TILE, 2 * G::A_TILE, &bar_a[s]);
-        }
-        copied = c + 1;
-        // B chunk: element pairs (k, k+1) of column n -> K-major core layout
-        // (adjacent halves of one 16-byte core row), hi and lo tiles
-        __half *bhi = reinterpret_cast<__half *>(st + 2 * G::A_TILE);
-        __half *blo = reinterpret_cast<__half *>(st + 2 * G::A_TILE + G::B_TILE);
-#pragma unroll
-        for (int it = 0; it < ITEMS; it++) {
-            int n, k2;
-            if (!item(it, n, k2)) continue;
-            const float2 v = cvt(raw[it], c * KC + 2 * k2, n);
-            __half h0, l0, h1, l1;
-            split_f16(v.x, h0, l0);
-            split_f16(v.y, h1, l1);
-            const uint32_t off = kmajor_off(n, 2 * k2, G::SBO) >> 1;
-            *reinterpret_cast<__half2 *>(bhi + off) = __halves2half2(h0, h1);
-            *reinterpret_cast<__half2 *>(blo + off) = __halves2half2(l0, l1);
-        }
-        if (c + 1 < nchunks) fetch(c + 1);     // in flight while this chunk's MMAs are issued
-        fence_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            if (!mbar_wait(&bar_a[s], (c >> 1) & 1, kMaxPolls)) {
-                *abort_sh = 1;
-            } else {
-                fence_after_sync();
-                const uint32_t a0 = smem_addr(st), b0 = smem_addr(st + 2 * G::A_TILE);
+    // the control warps stay converged: lane 0 acts, the other lanes wait at
+    // the shuffle instead of polling a barrier beside it
+    if (warp == 0) {                                      // MMA issuer
+        for (int c = 0; c < nchunks; c++) {
+            const int s = c % NS;
+            int okw = 1;
+            if (lane == 0) {
+                if (*abort_sh || !mbar_wait(&full[s], (c / NS) & 1, kMaxPolls)) {
+                    *abort_sh = 1;
+                    okw = 0;
+                } else {
+                    fence_after_sync();
+                    uint8_t *st = tc_smem + (size_t)s * G::STAGE;
+                    const uint32_t a0 = smem_addr(st), b0 = smem_addr(st + 2 * G::A_TILE);
+                    const uint64_t bh = sdesc(b0, 128, G::SBO), bl = sdesc(b0 + G::B_TILE, 128, G::SBO);
 #pragma unroll 1
-                for (int t = 0; t < MT; t++) {
-#pragma unroll 1
-                    for (int j = 0; j < KC / 16; j++) {
-                        const uint32_t aoff = (uint32_t)t * 16u * G::SBO + (uint32_t)j * 256u;
-                        const uint32_t boff = (uint32_t)j * 256u;
-                        const uint64_t ahi = sdesc(a0 + aoff, 128, G::SBO);
-                        const uint64_t alo = sdesc(a0 + G::A_TILE + aoff, 128, G::SBO);
-                        const uint64_t bh = sdesc(b0 + boff, 128, G::SBO);
-                        const uint64_t bl = sdesc(b0 + G::B_TILE + boff, 128, G::SBO);
-                        const uint32_t d = tmem + (uint32_t)(t * NT);
-                        const uint32_t acc0 = (c > 0 || j > 0) ? 1u : 0u;
-                        mma_f16(d, ahi, bh, idesc, acc0);
-                        mma_f16(d, ahi, bl, idesc, 1u);
-                        mma_f16(d, alo, bh, idesc, 1u);
+                    for (int t = 0; t < MT; t++) {
+#pragma unroll
+                        for (int j = 0; j < KC / 16; j++) {
+                            const uint32_t aoff = (uint32_t)t * 16u * G::SBO + (uint32_t)j * 256u;
+                            const uint64_t ahi = sdesc(a0 + aoff, 128, G::SBO);
+                            const uint64_t alo = sdesc(a0 + G::A_TILE + aoff, 128, G::SBO);
+                            const uint64_t bhj = bh + (uint64_t)((j * 256u) >> 4), blj = bl + (uint64_t)((j * 256u) >> 4);
+                            const uint32_t d = tmem + (uint32_t)(t * NT);
+                            mma_f16(d, ahi, bhj, idesc, (c > 0 || j > 0) ? 1u : 0u);
+                            mma_f16(d, ahi, blj, idesc, 1u);
+                            mma_f16(d, alo, bhj, idesc, 1u);
+                        }
                     }
+                    mma_commit(&empty[s]);
                 }
-                mma_commit(&bar_mma[s]);
             }
+            if (!__shfl_sync(0xffffffffu, okw, 0)) break;
         }
-        __syncthreads();
-        if (*abort_sh) break;
-        issued = c + 1;
+        if (lane == 0) mma_commit(done);                  // everything issued so far, done or not
+        __syncwarp();
+    } else if (warp == 1) {                               // A producer
+        for (int c = 0; c < nchunks; c++) {
+            const int s = c % NS;
+            int okw = 1;
+            if (lane == 0) {
+                if (c >= NS && (*abort_sh || !mbar_wait(&empty[s], (c / NS - 1) & 1, kMaxPolls))) {
+                    *abort_sh = 1;
+                    okw = 0;
+                } else {
+                    uint8_t *st = tc_smem + (size_t)s * G::STAGE;
+                    mbar_expect_tx(&full[s], 2 * G::A_TILE);
+                    bulk_g2s(st, a_prep + (size_t)c * 2 * G::A_TILE, 2 * G::A_TILE, &full[s]);
+                }
+            }
+            if (!__shfl_sync(0xffffffffu, okw, 0)) break;
+        }
+    } else {                                              // B producers
+        // loads run two chunks ahead of the stores (register ring of depth 2,
+        // the loop unrolled by two so the ring index is static)
+        const int p = tid - 64;
+        using Raw = decltype(load(0, 0));
+        Raw ra[ITEMS], rb[ITEMS];
+        auto fetch = [&](Raw *r, int c) {
+            if (c >= nchunks) return;
+#pragma unroll
+            for (int it = 0; it < ITEMS; it++) {
+                const int i = p + it * G::PRODUCERS;
+                const int n = K_FAST ? i / (KC / 2) : i % NT, k2 = K_FAST ? i % (KC / 2) : i / NT;
+                if (i < PAIRS) r[it] = load(c * KC + 2 * k2, n);
+            }
+        };
+        // wait for stage s (warp-uniform), store chunk c from r, publish it
+        auto put = [&](Raw *r, int c) -> bool {
+            const int s = c % NS;
+            if (c >= NS) {
+                int okw = 1;
+                if (lane == 0) okw = (!*abort_sh && mbar_wait(&empty[s], (c / NS - 1) & 1, kMaxPolls)) ? 1 : 0;
+                okw = __shfl_sync(0xffffffffu, okw, 0);
+                if (!okw) { if (lane == 0) *abort_sh = 1; return false; }
+            }
+            uint8_t *st = tc_smem + (size_t)s * G::STAGE;
+            __half *bhi = reinterpret_cast<__half *>(st + 2 * G::A_TILE);
+            __half *blo = reinterpret_cast<__half *>(st + 2 * G::A_TILE + G::B_TILE);
+#pragma unroll
+            for (int it = 0; it < ITEMS; it++) {
+                const int i = p + it * G::PRODUCERS;
+                if (i >= PAIRS) continue;
+                const int n = K_FAST ? i / (KC / 2) : i % NT, k2 = K_FAST ? i % (KC / 2) : i / NT;
+                const float2 v = cvt(r[it], c * KC + 2 * k2, n);
+                __half h0, l0, h1, l1;
+                split_f16(v.x, h0, l0);
+                split_f16(v.y, h1, l1);
+                const uint32_t off = kmajor_off(n, 2 * k2, G::SBO) >> 1;
+                *reinterpret_cast<__half2 *>(bhi + off) = __halves2half2(h0, h1);
+                *reinterpret_cast<__half2 *>(blo + off) = __halves2half2(l0, l1);
+            }
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[s]);          // one arrival per producer warp
+            return true;
+        };
+        fetch(ra, 0);
+        fetch(rb, 1);
+        for (int c = 0; c < nchunks; c += 2) {
+            if (!put(ra, c)) break;
+            fetch(ra, c + 2);
+            if (c + 1 >= nchunks) break;
+            if (!put(rb, c + 1)) break;
+            fetch(rb, c + 3);
+        }
     }
-    // all committed MMAs done (bounded), then the accumulator is read back
-    bool ok = !*abort_sh;
-    if (issued > 0 && !mbar_wait(&bar_mma[(issued - 1) & 1], ((issued - 1) >> 1) & 1, kMaxPolls)) ok = false;
-    if (issued > 1 && !mbar_wait(&bar_mma[(issued - 2) & 1], ((issued - 2) >> 1) & 1, kMaxPolls)) ok = false;
-    // an A copy started for a chunk whose MMAs never ran: let it land first
-    if (copied > issued && tid == 0) (void)mbar_wait(&bar_a[(copied - 1) & 1], ((copied - 1) >> 1) & 1, kMaxPolls);
+    // the accumulator is complete once `done` has fired (one decision for the CTA)
+    const int mine = mbar_wait(done, 0, kMaxPolls) ? 1 : 0;
+    const bool ok = __syncthreads_and(mine && !*abort_sh) != 0;
     fence_after_sync();
-    if (ok && issued == nchunks) {
-        // warp w reads lanes 32*(w%4); with 8 warps the two halves take
-        // alternate 16-column groups
-        constexpr int WG = NTHR / 128;
+    if (ok) {
 #pragma unroll 1
         for (int t = 0; t < MT; t++) {
 #pragma unroll 1
-            for (int n0 = 16 * (warp >> 2); n0 < NT; n0 += 16 * WG) {
+            for (int n0 = 16 * (warp >> 2); n0 < NT; n0 += 32) {
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(t * NT + n0), v);
                 epi(t * 128 + 32 * (warp & 3) + lane, n0, v);
@@ -195,6 +234,11 @@ __device__ void gemm_block(const uint8_t *__restrict__ a_prep, int K, Load load,
     fence_before_sync();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, G::TMEM_COLS);
+}
+
+template <int MT, int NT, int NS, int KC_ = 16>
+__host__ __device__ inline size_t ws_prepared_bytes(int K) {
+    return (size_t)(K / KC_) * 2 * WsGeom<MT, NT, NS, KC_>::A_TILE;
 }
 
 }  // namespace tc

@@ -77,12 +77,14 @@ static void *reader(void *arg)
     return NULL;
 }
 
+/* on a CUDA error: report it, and leave through the cleanup below */
 #define CK(call)                                                                  \
     do {                                                                          \
         cudaError_t e_ = (call);                                                  \
         if (e_ != cudaSuccess) {                                                  \
             fprintf(stderr, "xcorr: %s: %s\n", #call, cudaGetErrorString(e_));    \
-            return 1;                                                             \
+            failed = 1;                                                           \
+            goto cleanup;                                                         \
         }                                                                         \
     } while (0)
 
@@ -90,6 +92,16 @@ int xcli_correlate_streamed(const xcli *xc, xcg_ctx *ctx, xcg_result *host_resul
 {
     const int ns = xc->nyl, nxl = xc->nxl, npy = xc->npy;
     if (xc->nlocs == 0) return 0;
+    int failed = 0, started = 0;
+    ingest g;
+    memset(&g, 0, sizeof g);
+    g.fd[0] = g.fd[1] = -1;
+    void *d_img[2] = {NULL, NULL};
+    xcg_loc *d_locs = NULL;
+    xcg_result *d_res = NULL;
+    cudaStream_t st = NULL;
+    cudaEvent_t ev = NULL;
+    pthread_t th;
     /* lines each strip needs (exclusive end) and the first line anyone needs */
     int *need[2];
     need[0] = (int *)malloc(sizeof(int) * (size_t)ns);
@@ -107,8 +119,6 @@ int xcli_correlate_streamed(const xcli *xc, xcg_ctx *ctx, xcg_result *host_resul
             if (ys < first[1]) first[1] = ys;
         }
     }
-    ingest g;
-    memset(&g, 0, sizeof g);
     const char *names[2] = {xc->data1_name, xc->data2_name};
     g.nx[0] = xc->m_nx; g.ny[0] = xc->m_ny;
     g.nx[1] = xc->s_nx; g.ny[1] = xc->s_ny;
@@ -123,18 +133,12 @@ int xcli_correlate_streamed(const xcli *xc, xcg_ctx *ctx, xcg_result *host_resul
         if (nb > total) total = nb;
     }
     g.nbands = total;
+    pthread_mutex_init(&g.mu, NULL);
+    pthread_cond_init(&g.cv, NULL);
     for (int s = 0; s < NSLOT; s++) {
         g.ready[s] = -1;
         for (int k = 0; k < 2; k++) CK(cudaMallocHost((void **)&g.buf[s][k], (size_t)g.band * g.nx[k] * 4));
     }
-    pthread_mutex_init(&g.mu, NULL);
-    pthread_cond_init(&g.cv, NULL);
-
-    void *d_img[2];
-    xcg_loc *d_locs;
-    xcg_result *d_res;
-    cudaStream_t st;
-    cudaEvent_t ev;
     CK(cudaMalloc(&d_img[0], (size_t)g.nx[0] * g.ny[0] * 4));
     CK(cudaMalloc(&d_img[1], (size_t)g.nx[1] * g.ny[1] * 4));
     CK(cudaMalloc((void **)&d_locs, sizeof(xcg_loc) * (size_t)xc->nlocs));
@@ -143,9 +147,9 @@ int xcli_correlate_streamed(const xcli *xc, xcg_ctx *ctx, xcg_result *host_resul
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     CK(cudaMemcpyAsync(d_locs, xc->loc, sizeof(xcg_loc) * (size_t)xc->nlocs, cudaMemcpyHostToDevice, st));
 
-    pthread_t th;
     pthread_create(&th, NULL, reader, &g);
-    int next = 0, failed = 0;
+    started = 1;
+    int next = 0;
     for (int b = 0; b <= g.nbands && !failed; b++) {
         int avail[2];
         if (b < g.nbands) {
@@ -192,21 +196,27 @@ int xcli_correlate_streamed(const xcli *xc, xcg_ctx *ctx, xcg_result *host_resul
             next = last;
         }
     }
-    pthread_mutex_lock(&g.mu);
-    g.stop = 1;
-    pthread_cond_broadcast(&g.cv);
-    pthread_mutex_unlock(&g.mu);
-    pthread_join(th, NULL);
     if (!failed) {
         CK(cudaMemcpyAsync(host_results, d_res, sizeof(xcg_result) * (size_t)xc->nlocs, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
     }
+cleanup:
+    if (started) {
+        pthread_mutex_lock(&g.mu);
+        g.stop = 1;
+        pthread_cond_broadcast(&g.cv);
+        pthread_mutex_unlock(&g.mu);
+        pthread_join(th, NULL);
+    }
+    if (st) cudaStreamSynchronize(st);
     for (int s = 0; s < NSLOT; s++)
-        for (int k = 0; k < 2; k++) cudaFreeHost(g.buf[s][k]);
+        for (int k = 0; k < 2; k++)
+            if (g.buf[s][k]) cudaFreeHost(g.buf[s][k]);
     cudaFree(d_img[0]); cudaFree(d_img[1]); cudaFree(d_locs); cudaFree(d_res);
-    cudaEventDestroy(ev);
-    cudaStreamDestroy(st);
-    close(g.fd[0]); close(g.fd[1]);
+    if (ev) cudaEventDestroy(ev);
+    if (st) cudaStreamDestroy(st);
+    for (int k = 0; k < 2; k++)
+        if (g.fd[k] >= 0) close(g.fd[k]);
     free(need[0]); free(need[1]);
     return failed;
 }
