@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <complex>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -23,6 +24,11 @@
 #include "xcorr_ctx.cuh"
 
 using cd = std::complex<double>;
+
+// windows per row-stage sub-launch of the host-buffer entry
+#ifndef XCG_ROW_SUB
+#define XCG_ROW_SUB 128
+#endif
 
 namespace {
 
@@ -264,8 +270,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
             XCG_CK_C(cudaEventCreateWithFlags(&c->ev_join[k], cudaEventDisableTiming), "cudaEventCreate");
         }
         XCG_CK_C(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
-        for (int k = 0; k < 2; k++)
-            XCG_CK_C(cudaStreamCreateWithFlags(&c->copy_stream[k], cudaStreamNonBlocking), "cudaStreamCreate");
+        XCG_CK_C(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
     }
 #undef XCG_CK_C
     c->stats.scratch_bytes = c->scratch_bytes;
@@ -286,6 +291,7 @@ void xcg_destroy(xcg_ctx *c) {
     cudaFree(c->d_img[1]);
     cudaFree(c->d_locs);
     cudaFree(c->d_res);
+    if (c->h_io) cudaFreeHost(c->h_io);
     cudaFree(c->ref_feat);
     cudaFree(c->ref_pred);
     cudaFree(c->ref_skip);
@@ -297,8 +303,7 @@ void xcg_destroy(xcg_ctx *c) {
         if (c->ev_join[k]) cudaEventDestroy(c->ev_join[k]);
     }
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-    for (int k = 0; k < 2; k++)
-        if (c->copy_stream[k]) { cudaStreamSynchronize(c->copy_stream[k]); cudaStreamDestroy(c->copy_stream[k]); }
+    if (c->copy_stream) { cudaStreamSynchronize(c->copy_stream); cudaStreamDestroy(c->copy_stream); }
     for (cudaEvent_t ev : c->band_ready) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -377,6 +382,23 @@ static Plan with_slot(Plan P, size_t off) {
     return P;
 }
 
+// Windows [off, off + n) of batch plan P as a plan of their own, for the row
+// stage, whose kernel writes only the per-window arrays below.
+Plan rows_subrange(Plan P, int off, int n) {
+    const size_t o = (size_t)off;
+    P.locs += off;
+    if (P.winref) P.winref += off;
+    P.win0 += off;
+    P.nwin = n;
+    P.zrow += o * P.npy * P.npx;
+    P.amp1 += o * P.npy * P.npx;
+    P.amp2c += o * P.ny_corr * P.nx_corr;
+    P.part += o * 2 * P.nchunks;
+    P.oobmap += o * P.nchunks;
+    P.minmax += o * 4 * P.nchunks;
+    return P;
+}
+
 int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len) {
     int bw = c->max_batch;
     // enough windows for two batches of >= 256: split so the two slots overlap
@@ -387,8 +409,7 @@ int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len) {
     return bw;
 }
 
-xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s, const cudaEvent_t *ready,
-                      int nready) {
+xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s, const RowsHook &rows) {
     // launch slots: rows, columns, peak, subpixel; the precision form splits
     // the column stage into three tensor-core DFT stages
     const bool tcf = P.tc_form != 0;
@@ -422,11 +443,13 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
         if (Q.nwin > maxw) maxw = Q.nwin;
         Q.locs = locs0 + Q.win0;
         Q.winref = ref0 ? ref0 + Q.win0 : nullptr;
-        for (int k = 0; k < nready; k++) XCG_CK(cudaStreamWaitEvent(ss, ready[(size_t)b * nready + k], 0), "cudaStreamWaitEvent");
         for (int k = 0; k < nk; k++) {
             if (c->profiling) cudaEventRecord(c->events[ei++], ss);
             const bool tm = Q.corr_mode < 2;     // -time / -time4: full-search surface
-            if (tcf) {
+            if (k == 0 && rows) {
+                const xcg_status rs = rows(Q, ss);
+                if (rs != XCG_OK) return rs;
+            } else if (tcf) {
                 switch (k) {
                     case 0: launch_rows(Q, ss); break;
                     case 1: launch_tc_rows(Q, ss); break;
@@ -497,55 +520,85 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
         }
     }
     if (nlocs > c->io_cap) {
-        cudaFree(c->d_locs); cudaFree(c->d_res);
-        c->d_locs = nullptr; c->d_res = nullptr; c->io_cap = 0;
+        cudaFree(c->d_locs); cudaFree(c->d_res); cudaFreeHost(c->h_io);
+        c->d_locs = nullptr; c->d_res = nullptr; c->h_io = nullptr; c->io_cap = 0;
         XCG_CK(cudaMalloc(&c->d_locs, (size_t)nlocs * sizeof(xcg_loc)), "cudaMalloc locs");
         XCG_CK(cudaMalloc(&c->d_res, (size_t)nlocs * sizeof(xcg_result)), "cudaMalloc results");
+        // pinned staging for the locations and results: both copies stay asynchronous
+        XCG_CK(cudaHostAlloc(&c->h_io, (size_t)nlocs * (sizeof(xcg_loc) + sizeof(xcg_result)), cudaHostAllocDefault),
+               "cudaHostAlloc");
         c->io_cap = nlocs;
     }
+    xcg_loc *h_locs = reinterpret_cast<xcg_loc *>(c->h_io);
+    xcg_result *h_res = reinterpret_cast<xcg_result *>(h_locs + c->io_cap);
     cudaStream_t s = c->stream;
-    XCG_CK(cudaMemcpyAsync(c->d_locs, locs, (size_t)nlocs * sizeof(xcg_loc), cudaMemcpyHostToDevice, s), "copy locs");
-    // Copy the images in row bands, master and slave on their own streams:
-    // batch b waits only for the rows its windows read (master rows up to
-    // y + npy/2, slave rows up to y + y_offset + ishft + npy/2), so the copy of
-    // later rows overlaps the first batches' kernels.
+    XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");      // the staging buffer is free again
+    memcpy(h_locs, locs, (size_t)nlocs * sizeof(xcg_loc));
+    XCG_CK(cudaMemcpyAsync(c->d_locs, h_locs, (size_t)nlocs * sizeof(xcg_loc), cudaMemcpyHostToDevice, s), "copy locs");
+    // Copy the images in row bands on one stream and launch the row stage of
+    // each batch in sub-ranges of about XCG_ROW_SUB windows, each right after
+    // the copy of the rows its windows read (master rows y - npy/2 .. y + npy/2,
+    // slave rows shifted by y_offset + ishft), master band before slave band:
+    // only the first band's copy is exposed; later bands copy while earlier
+    // rows are transformed (a band copies in about half the time its rows'
+    // kernels take).  Rows no window reads are not copied.
     const int bw = xcg::ctx_batch_windows(c, nlocs, strip_len);
-    const int nb = (nlocs + bw - 1) / bw;
-    while (c->band_ready.size() < (size_t)nb * 2) {
-        cudaEvent_t ev;
-        XCG_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
-        c->band_ready.push_back(ev);
-    }
+    std::vector<int> bounds;
+    for (int w = 0; w < nlocs; w += bw) bounds.push_back(w);
+    bounds.push_back(nlocs);
+    const int nb = (int)bounds.size() - 1;
     XCG_CK(cudaEventRecord(c->ev_fork, s), "cudaEventRecord");     // after whatever the caller queued on s
-    for (int k = 0; k < 2; k++) XCG_CK(cudaStreamWaitEvent(c->copy_stream[k], c->ev_fork, 0), "cudaStreamWaitEvent");
+    XCG_CK(cudaStreamWaitEvent(c->copy_stream, c->ev_fork, 0), "cudaStreamWaitEvent");
     const int npy = c->base.npy;
     const int ny[2] = {m_ny, s_ny};
     const size_t rowb[2] = {(size_t)m_nx * es, (size_t)s_nx * es};
     const void *src[2] = {master, slave};
-    int done[2] = {0, 0};
-    std::vector<int> starts;
-    for (int b = 0; b < nb; b++) {
-        const int w0 = b * bw, w1 = (b + 1 == nb) ? nlocs : (b + 1) * bw;
-        starts.push_back(w0);
-        int want[2] = {0, 0};
+    // rows [lo, hi) of image k that windows [w0, w1) read
+    auto rows_of = [&](int w0, int w1, int k, int &lo, int &hi) {
+        lo = ny[k]; hi = 0;
         for (int w = w0; w < w1; w++) {
-            const int y = locs[w].y, ishft = (int)((double)y * astretcha);
-            want[0] = std::max(want[0], y + npy / 2 + 1);
-            want[1] = std::max(want[1], y + y_offset + ishft + npy / 2 + 1);
+            const int y = locs[w].y;
+            const int y0 = k == 0 ? y - npy / 2 : y + y_offset + (int)((double)y * astretcha) - npy / 2;
+            lo = std::min(lo, std::max(y0, 0));
+            hi = std::max(hi, std::min(y0 + npy, ny[k]));
         }
-        if (b + 1 == nb) { want[0] = ny[0]; want[1] = ny[1]; }
-        for (int k = 0; k < 2; k++) {
-            const int to = std::min(std::max(want[k], done[k]), ny[k]);
-            if (to > done[k])
-                XCG_CK(cudaMemcpyAsync((char *)c->d_img[k] + (size_t)done[k] * rowb[k], (const char *)src[k] + (size_t)done[k] * rowb[k],
-                                       (size_t)(to - done[k]) * rowb[k], cudaMemcpyHostToDevice, c->copy_stream[k]),
-                       k ? "copy slave" : "copy master");
-            done[k] = to;
-            XCG_CK(cudaEventRecord(c->band_ready[(size_t)b * 2 + k], c->copy_stream[k]), "cudaEventRecord");
-        }
+    };
+    int done[2];
+    for (int k = 0; k < 2; k++) {
+        int lo, hi;
+        rows_of(0, nlocs, k, lo, hi);
+        done[k] = lo;            // bands grow from the first row any window reads
     }
-    starts.push_back(nlocs);
-    XCG_CK(cudaSetDevice(c->device), "cudaSetDevice");
+    size_t nev = 0;
+    auto rows_hook = [&](const xcg::Plan &Q, cudaStream_t ss) -> xcg_status {
+        const int nsub = std::max(1, (Q.nwin + XCG_ROW_SUB / 2) / XCG_ROW_SUB);
+        for (int j = 0; j < nsub; j++) {
+            const int o0 = (int)((long long)Q.nwin * j / nsub), o1 = (int)((long long)Q.nwin * (j + 1) / nsub);
+            if (o1 <= o0) continue;
+            for (int k = 0; k < 2; k++) {
+                int lo, hi;
+                rows_of(Q.win0 + o0, Q.win0 + o1, k, lo, hi);
+                if (hi > done[k]) {
+                    XCG_CK(cudaMemcpyAsync((char *)c->d_img[k] + (size_t)done[k] * rowb[k],
+                                           (const char *)src[k] + (size_t)done[k] * rowb[k],
+                                           (size_t)(hi - done[k]) * rowb[k], cudaMemcpyHostToDevice, c->copy_stream),
+                           k ? "copy slave" : "copy master");
+                    done[k] = hi;
+                }
+            }
+            if (c->band_ready.size() <= nev) {
+                cudaEvent_t ev;
+                XCG_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+                c->band_ready.push_back(ev);
+            }
+            XCG_CK(cudaEventRecord(c->band_ready[nev], c->copy_stream), "cudaEventRecord");
+            XCG_CK(cudaStreamWaitEvent(ss, c->band_ready[nev], 0), "cudaStreamWaitEvent");
+            nev++;
+            xcg::launch_rows(xcg::rows_subrange(Q, o0, o1 - o0), ss);
+        }
+        c->stats.launches += nsub - 1;       // ctx_launch counts the row stage once
+        return XCG_OK;
+    };
     memset(&c->stats, 0, sizeof c->stats);
     c->stats.scratch_bytes = c->scratch_bytes;
     xcg::Plan P = xcg::ctx_plan(c);
@@ -559,15 +612,16 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     P.pairs = nullptr;
     P.winref = nullptr;
     P.locs = c->d_locs;
-    xcg_status st = xcg::ctx_launch(c, P, starts.data(), nb, s, c->band_ready.data(), 2);
+    xcg_status st = xcg::ctx_launch(c, P, bounds.data(), nb, s, rows_hook);
     if (st != XCG_OK) return st;
-    XCG_CK(cudaMemcpyAsync(results, c->d_res, (size_t)nlocs * sizeof(xcg_result), cudaMemcpyDeviceToHost, s), "copy results");
+    XCG_CK(cudaMemcpyAsync(h_res, c->d_res, (size_t)nlocs * sizeof(xcg_result), cudaMemcpyDeviceToHost, s), "copy results");
     XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     if (c->base.tc_form && c->tc_err) {     // a tensor-core wait that ran out leaves its block unwritten
         int herr = 0;
         XCG_CK(cudaMemcpy(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost), "read tensor-core status");
         if (herr) { xcg::set_last_error("tensor-core stage: a wait ran out"); return XCG_ERR_CUDA; }
     }
+    memcpy(results, h_res, (size_t)nlocs * sizeof(xcg_result));
     return XCG_OK;
 }
 

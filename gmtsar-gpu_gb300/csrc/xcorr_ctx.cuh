@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <vector>
 
 #include "xcorr_gb300.h"
@@ -23,10 +24,10 @@ struct xcg_ctx {
     int nslots = 2;
     cudaStream_t slot_stream[2] = {nullptr, nullptr};
     cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
-    // host entry: the two images are copied on their own streams in row bands,
-    // one band per batch, and each batch waits only for its band
-    cudaStream_t copy_stream[2] = {nullptr, nullptr};
-    std::vector<cudaEvent_t> band_ready;      // [batch][2]
+    // host entry: the two images are copied on one stream in row bands, and
+    // each row-stage sub-launch waits only for its band
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaEvent_t> band_ready;      // one per band of a call
     size_t off_zrow, off_amp1, off_amp2c, off_part, off_oob, off_minmax, off_means, off_qspec, off_surf, off_md,
         off_mdnext, off_corr0n;
     // host-entry buffers
@@ -34,6 +35,7 @@ struct xcg_ctx {
     size_t img_bytes[2] = {0, 0};
     xcg_loc *d_locs = nullptr;
     xcg_result *d_res = nullptr;
+    void *h_io = nullptr;         // pinned: io_cap locations, then io_cap results
     int io_cap = 0;
     cudaStream_t stream = nullptr;
     // optional per-window 9x9 neighbourhoods written by xcg_correlate_device
@@ -55,13 +57,17 @@ namespace xcg {
 // The context's plan with its tables and scratch filled in; the caller sets
 // the pair fields, the window arrays and launches with ctx_launch.
 Plan ctx_plan(const xcg_ctx *c);
+// Launches the row stage of one batch (plan Q) on stream ss in place of the
+// single row launch; the host entry copies image bands between sub-launches.
+using RowsHook = std::function<xcg_status(const Plan &Q, cudaStream_t ss)>;
 // Launch the four kernels for windows [starts[b], starts[b+1]) of the
 // window arrays in P (locs, winref), b < nbatch; updates the context stats.
-// ready (optional): nready events per batch that batch b waits for first.
 xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nbatch, cudaStream_t s,
-                      const cudaEvent_t *ready = nullptr, int nready = 0);
+                      const RowsHook &rows = {});
 // Windows per batch xcg_correlate_device uses for nlocs windows.
 int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len);
+// Windows [off, off + n) of batch plan P, for a row-stage sub-launch.
+Plan rows_subrange(Plan P, int off, int n);
 void set_last_error(const char *msg);
 // precision form (tc_dft.cu)
 xcg_status tc_enable(xcg_ctx *c);

@@ -599,14 +599,22 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
     const float *a2 = P.amp2c + (size_t)w * P.ny_corr * P.nx_corr;
     long long sn = 0, s1 = 0, s2 = 0;
     constexpr int NXC = N / 2;          // nx_corr = 2 xsearch = npx / 2
-    for (int i = threadIdx.x; i < P.ny_corr * NXC; i += NT) {
-        const int r = i / NXC, cc = i - r * NXC;
-        float va = a1[(size_t)r * N + cc] - m1f;
-        va = va * 1.0f;
-        float vb = a2[i] - m2f;
-        vb = vb * 1.0f;
-        const long long ia = (long long)(int)va, ib = (long long)(int)vb;
-        sn += ia * ib; s1 += ia * ia; s2 += ib * ib;
+    constexpr int GU = 8;               // loads in flight per thread and operand
+    const int ntot = P.ny_corr * NXC;   // a multiple of NT * GU (ny_corr >= 64, NXC >= 64)
+    for (int i0 = threadIdx.x; i0 < ntot; i0 += NT * GU) {
+        float va[GU], vb[GU];
+#pragma unroll
+        for (int u = 0; u < GU; u++) {
+            const int i = i0 + u * NT;
+            const int r = i / NXC, cc = i - r * NXC;
+            va[u] = __ldg(a1 + (size_t)r * N + cc);
+            vb[u] = __ldg(a2 + i);
+        }
+#pragma unroll
+        for (int u = 0; u < GU; u++) {
+            const long long ia = (long long)(int)(va[u] - m1f), ib = (long long)(int)(vb[u] - m2f);
+            sn += ia * ib; s1 += ia * ia; s2 += ib * ib;
+        }
     }
     sn = warp_sum_i64(sn); s1 = warp_sum_i64(s1); s2 = warp_sum_i64(s2);
     if (l32 == 0) { ri64[warp] = sn; ri64[8 + warp] = s1; ri64[16 + warp] = s2; }

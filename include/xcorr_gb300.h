@@ -108,7 +108,9 @@ void xcg_destroy(xcg_ctx *ctx);
  * The slave window of location (x,y) starts at x + x_offset - npx/2,
  * y + y_offset + (int)(y*astretcha) - npy/2 (read_xcorr_data.c:65-75, xcorr.cu:332-333).
  * strip_len: locations per strip (nxl) for the one cross-window read the
- * reference makes; 0 disables it.  Synchronous. */
+ * reference makes; 0 disables it.  Synchronous.  Only the image lines the
+ * windows read are copied to the device, in bands that overlap the kernels;
+ * page-locked (pinned) image buffers make those copies asynchronous. */
 xcg_status xcg_correlate(xcg_ctx *ctx,
                          const void *master, int32_t m_nx, int32_t m_ny,
                          const void *slave, int32_t s_nx, int32_t s_ny,

@@ -1,0 +1,72 @@
+"""The host-buffer entry (xcg_correlate) against the device entry on the same
+windows: it copies only the image rows the windows read, in bands that each
+batch waits for, so its results must not depend on the location order, on
+the part of the image the windows cover, or on what an earlier call left in
+the context's image buffers.  Bar: every result field bit-identical to
+xcg_correlate_device on fully resident images."""
+import numpy as np
+import pytest
+import torch
+
+import xcorr_gb300 as xg
+from xcorr_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _device(ctx, m, s, locs, strip_len, y_offset=0, astretcha=0.0):
+    dev = torch.device("cuda", 0)
+    dm, ds = torch.from_numpy(m).to(dev), torch.from_numpy(s).to(dev)
+    dl = torch.from_numpy(np.ascontiguousarray(locs, np.int32)).to(dev)
+    dr = torch.zeros((len(locs), xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+    ctx.correlate_device(dm.data_ptr(), m.shape[1], m.shape[0], ds.data_ptr(), s.shape[1], s.shape[0],
+                         dl.data_ptr(), len(locs), dr.data_ptr(), 0, y_offset=y_offset, astretcha=astretcha,
+                         strip_len=strip_len)
+    torch.cuda.synchronize()
+    return np.frombuffer(dr.cpu().numpy().tobytes(), dtype=xg.RESULT_DTYPE)
+
+
+def _same(a, b):
+    assert a.tobytes() == b.tobytes()
+
+
+@pytest.fixture(scope="module")
+def pairs():
+    p1 = synth.make_pair(synth.PairSpec(nx=1024, ny=3072, dx=1.3, dy=-2.2, noise_frac=0.1, seed=21))
+    p2 = synth.make_pair(synth.PairSpec(nx=1024, ny=3072, dx=-0.6, dy=3.1, noise_frac=0.2, seed=22))
+    return p1, p2
+
+
+def test_sub_area_and_stale_buffers(pairs):
+    (m1, s1), (m2, s2) = pairs
+    full = xg.grid(1024, 3072, 6, 30, 64, 64)
+    part = full[(full[:, 1] > 1200) & (full[:, 1] < 2000)]        # a band of strips in the middle
+    with xg.Context(xg.params(64, 64), max_batch=96) as ctx:
+        ctx.correlate(m1, s1, full, strip_len=6)                  # fills the image buffers with pair 1
+        r = ctx.correlate(m2, s2, part, strip_len=6)              # reads only pair 2's rows it copies
+        d = _device(ctx, m2, s2, part, 6)
+    _same(r, d)
+
+
+def test_location_order_and_shifted_slave(pairs):
+    (m1, s1), _ = pairs
+    locs = xg.grid(1024, 3072, 6, 30, 64, 64)
+    rng = np.random.default_rng(5)
+    strips = rng.permutation(len(locs) // 6)
+    shuffled = np.concatenate([locs[6 * k:6 * k + 6] for k in strips])   # whole strips, any order
+    for y_offset, ast in ((0, 0.0), (-37, 0.0), (12, 0.004)):
+        with xg.Context(xg.params(64, 64), max_batch=64) as ctx:
+            r = ctx.correlate(m1, s1, shuffled, 0, y_offset, ast, strip_len=6)
+            st = ctx.stats()
+            d = _device(ctx, m1, s1, shuffled, 6, y_offset, ast)
+        assert st.batches >= 3
+        _same(r, d)
+
+
+def test_single_strip_job(pairs):
+    (m1, s1), _ = pairs
+    locs = xg.grid(1024, 3072, 6, 30, 64, 64)[-6:]                 # the last strip only
+    with xg.Context(xg.params(64, 64)) as ctx:
+        r = ctx.correlate(m1, s1, locs, strip_len=6)
+        d = _device(ctx, m1, s1, locs, 6)
+    _same(r, d)
