@@ -180,7 +180,27 @@ namespace xcg {
 
 __host__ __device__ constexpr int fft_lanes(int n) { return (n / 16 < 32) ? n / 16 : 32; }
 
-template <int N, int DIR, int PASS>
+// cos(2 pi k / 32) and sin(2 pi k / 32), any integer k
+__host__ __device__ constexpr float cos32_oct(int k) {      // k in 0..8
+    return k == 0 ? 1.0f : k == 1 ? 0.980785280403230449126f : k == 2 ? 0.923879532511286756128f
+         : k == 3 ? 0.831469612302545237079f : k == 4 ? 0.707106781186547524401f : k == 5 ? 0.555570233019602224743f
+         : k == 6 ? 0.382683432365089771728f : k == 7 ? 0.195090322016128267848f : 0.0f;
+}
+__host__ __device__ constexpr float cos32(int k) {
+    k = ((k % 32) + 32) % 32;
+    return k <= 8 ? cos32_oct(k) : k <= 16 ? -cos32_oct(16 - k) : k <= 24 ? -cos32_oct(k - 16) : cos32_oct(32 - k);
+}
+__host__ __device__ constexpr float sin32(int k) { return cos32(k - 8); }
+
+// HS (half-sample shift, inverse transforms of N <= 256 only): the input
+// element f = lane + T*m is first multiplied by phi(f) = exp(i pi f'/N) / N
+// (f' = f, or f - N for f >= N/2), which turns the inverse FFT into the
+// half-sample shifted interpolation.  phi(f) = A(lane) * C(m): C(m) =
+// exp(2 pi i m / 32) / N, negated for m >= 8, is a constant multiplied here;
+// A(lane) = exp(i pi lane / N) rides on the next pass's twiddles (the pass-0
+// outputs of lane l are the next pass's inputs r = l), whose table must then
+// hold exp(-2 pi i r (k + 1/2) / N) (half_shift_twiddles).
+template <int N, int DIR, int PASS, bool HS = false>
 __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const float2 *tw, int Ns, int lane) {
     constexpr int T = fft_lanes(N);
     constexpr int NP = fft_npasses(N);
@@ -188,6 +208,7 @@ __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const f
     constexpr int NR = N / R;
     constexpr int IT = NR / T;                 // butterflies per lane in this pass
     static_assert(IT * R * T == N, "team layout");
+    static_assert(!HS || (DIR > 0 && N / T == 16 && IT == 1 && NP == 2), "half-sample shift: N = 128 or 256");
     if constexpr (PASS == 0) {
         // inputs from registers: element (lane + T*it) + NR*r = lane + T*(it + r*IT)
 #pragma unroll
@@ -195,6 +216,14 @@ __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const f
             float2 u[R];
 #pragma unroll
             for (int r = 0; r < R; r++) u[r] = v[it + r * IT];
+            if constexpr (HS) {
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const int k32 = r < 8 ? r : r + 16;          // m = r; the sign flip is +16/32 of a turn
+                    const float c = cos32(k32) / (float)N, s = sin32(k32) / (float)N;
+                    u[r] = make_float2(u[r].x * c - u[r].y * s, u[r].x * s + u[r].y * c);
+                }
+            }
             dft_reg<R, DIR>(u);
             const int j = lane + T * it;
 #pragma unroll
@@ -246,6 +275,13 @@ __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const f
 template <int N, int DIR>
 __device__ __forceinline__ void team_fft_reg(float2 *v, float2 *ex, const float2 *tw, int lane) {
     team_fft_reg_pass<N, DIR, 0>(v, ex, tw, 1, lane);
+}
+
+// Inverse FFT of X[f] * exp(i pi f' / N) / N (the odd samples of a 2x
+// zero-pad interpolation) for N = 128 or 256; twh: half_shift_twiddles(N).
+template <int N>
+__device__ __forceinline__ void team_ifft_half_shift(float2 *v, float2 *ex, const float2 *twh, int lane) {
+    team_fft_reg_pass<N, +1, 0, true>(v, ex, twh, 1, lane);
 }
 
 }  // namespace xcg

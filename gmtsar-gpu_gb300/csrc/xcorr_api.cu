@@ -202,12 +202,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
     // tables
     std::vector<float2> tw_row = stockham_twiddles(B.npx), tw_col = stockham_twiddles(B.npy);
     std::vector<float2> phase((size_t)(B.ri > 1 ? B.ri - 1 : 1) * B.npx);
-    for (int q = 1; q < B.ri; q++)
-        for (int f = 0; f < B.npx; f++) {
-            const int fp = (f < B.npx / 2) ? f : f - B.npx;
-            const cd v = std::polar(1.0 / B.npx, 2.0 * M_PI * fp * q / ((double)B.ri * B.npx));
-            phase[(size_t)(q - 1) * B.npx + f] = make_float2((float)v.real(), (float)v.imag());
-        }
+    xcg::put_row_phase(phase.data(), B.npx, B.ri);
     std::vector<float2> bx = box_spectrum(B.npx, xs), by = box_spectrum(B.npy, ys);
     std::vector<float2> kxo = interp_operator(B.n2x, B.nx2), kyo = interp_operator(B.n2y, B.ny2);
     std::vector<float2> all;

@@ -148,20 +148,27 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     constexpr int TWL = fft_twiddle_len(N);
     constexpr int PER = N / T;
 
+    // ri = 2 rows of up to 256 points: the phase of the interpolation rides
+    // on a second twiddle table (team_ifft_half_shift)
+    constexpr bool HSHIFT = (LG == 1) && (N <= 256);
+    constexpr int TWS = (N <= 256) ? 2 * TWL : TWL;     // twiddle entries in shared memory
+
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
     const int lane = l32 % T;
     const int tm = l32 / T;                             // team within the warp
     const int team = warp * TPW + tm;
-    char *tbase = reinterpret_cast<char *>(tw + TWL) + (size_t)team * (PADN * sizeof(float2) + 2 * N * sizeof(float));
+    char *tbase = reinterpret_cast<char *>(tw + TWS) + (size_t)team * (PADN * sizeof(float2) + 2 * N * sizeof(float));
     float2 *ex = reinterpret_cast<float2 *>(tbase);
     float *rb = reinterpret_cast<float *>(ex + PADN);    // [2][N] amplitudes in natural order
-    float *acc = reinterpret_cast<float *>(reinterpret_cast<char *>(tw + TWL) +
+    float *acc = reinterpret_cast<float *>(reinterpret_cast<char *>(tw + TWS) +
                                            (size_t)(blockDim.x / T) * (PADN * sizeof(float2) + 2 * N * sizeof(float))) +
                  (size_t)warp * 2 * ACC;                 // [2][ACC] first-level sums of the warp's chunk
 
     for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_row[i];
+    if constexpr (HSHIFT)
+        for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[TWL + i] = P.phase[i];
     __syncthreads();
 
     const int w = blockIdx.y;
@@ -242,10 +249,14 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
                 to_complex(again, v);
             }
             team_fft_reg<N, -1>(v, ex, tw, lane);
-            const float2 *ph = P.phase + (size_t)(p - 1) * N;
+            if constexpr (HSHIFT) {
+                team_ifft_half_shift<N>(v, ex, tw + TWL, lane);
+            } else {
+                const float2 *ph = P.phase + (size_t)(p - 1) * N;
 #pragma unroll
-            for (int m = 0; m < PER; m++) v[m] = cmulf(v[m], __ldg(ph + lane + T * m));
-            team_fft_reg<N, +1>(v, ex, tw, lane);
+                for (int m = 0; m < PER; m++) v[m] = cmulf(v[m], __ldg(ph + lane + T * m));
+                team_fft_reg<N, +1>(v, ex, tw, lane);
+            }
 #pragma unroll
             for (int m = KM0; m < KM1; m++) {
                 const int k = ((lane + T * m) << LG) + p - N / 2;
@@ -843,12 +854,37 @@ void launch_decide(const Plan &P, const float *pred, unsigned char *skip, float 
 
 // ---------------------------------------------------------------- launchers
 
+int put_row_phase(float2 *dst, int n, int ri) {
+    if (ri == 1) { dst[0] = make_float2(0.f, 0.f); return 1; }
+    if (ri == 2 && n <= 256) {
+        // [(r-1)*16 + k] = exp(-2 pi i r (k + 1/2) / n): the second pass's
+        // twiddle with the lane factor exp(i pi r / n) folded in
+        const int r1 = n / 16;                       // radix of the second pass
+        int o = 0;
+        for (int r = 1; r < r1; r++)
+            for (int k = 0; k < 16; k++) {
+                const double a = -2.0 * M_PI * r * (k + 0.5) / n;
+                dst[o++] = make_float2((float)cos(a), (float)sin(a));
+            }
+        for (; o < n; o++) dst[o] = make_float2(0.f, 0.f);
+        return n;
+    }
+    int o = 0;
+    for (int q = 1; q < ri; q++)
+        for (int f = 0; f < n; f++) {
+            const int fp = (f < n / 2) ? f : f - n;
+            const double a = 2.0 * M_PI * fp * q / ((double)ri * n);
+            dst[o++] = make_float2((float)(cos(a) / n), (float)(sin(a) / n));
+        }
+    return o;
+}
+
 template <int N>
 static size_t rows_smem() {
     constexpr int T = fft_lanes(N);
     constexpr int ACC = (N >= 1024) ? 1024 : 512;
     const int teams = 128 / T;
-    return fft_twiddle_len(N) * sizeof(float2) +
+    return fft_twiddle_len(N) * (N <= 256 ? 2 : 1) * sizeof(float2) +
            (size_t)teams * (fft_padded_len(N) * sizeof(float2) + 2 * N * sizeof(float)) +
            (size_t)(128 / 32) * 2 * ACC * sizeof(float);
 }

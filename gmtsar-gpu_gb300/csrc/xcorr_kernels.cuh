@@ -13,4 +13,9 @@ void launch_subpix(const Plan &P, cudaStream_t s);
 void launch_decide(const Plan &P, const float *pred, unsigned char *skip, float max_sigma, float max_dis,
                    cudaStream_t s);
 void set_last_error(const char *msg);
+// Range-interpolation table of the row kernel for n-point rows and factor ri
+// (Plan::phase), written to dst; returns the entries written, (ri-1)*n (1
+// for ri = 1).  For ri = 2 and n <= 256 it holds the half-shift twiddles of
+// team_ifft_half_shift, else the phase factors exp(2 pi i f' p/(ri n))/n.
+int put_row_phase(float2 *dst, int n, int ri);
 }  // namespace xcg

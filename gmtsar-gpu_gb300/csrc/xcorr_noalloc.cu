@@ -164,15 +164,7 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
     auto align = [&]() { o = (o + 31) & ~(size_t)31; };     // 256-byte boundaries
     o_twr = o; o += put_twiddles(t_tables + o, P.npx); align();
     o_twc = o; o += put_twiddles(t_tables + o, P.npy); align();
-    o_ph = o;
-    for (int q = 1; q < P.ri; q++)
-        for (int f = 0; f < P.npx; f++) {
-            const int fp = (f < P.npx / 2) ? f : f - P.npx;
-            const double a = 2.0 * M_PI * fp * q / ((double)P.ri * P.npx);
-            t_tables[o++] = make_float2((float)(cos(a) / P.npx), (float)(sin(a) / P.npx));
-        }
-    if (P.ri == 1) t_tables[o++] = make_float2(0.f, 0.f);
-    align();
+    o_ph = o; o += xcg::put_row_phase(t_tables + o, P.npx, P.ri); align();
     o_bx = o; o += put_box(t_tables + o, P.npx, xs); align();
     o_by = o; o += put_box(t_tables + o, P.npy, ys); align();
     o_kx = o; o += put_interp(t_tables + o, P.n2x, P.nx2); align();
