@@ -104,12 +104,13 @@ __device__ __forceinline__ float2 load_sample(const Plan &P, const void *img, in
 // (sqrt.approx.f32) stands in for the correctly rounded sqrtf, whose
 // special-case branch cost k_rows 7% of its instructions.  Measured on GB300
 // against sqrtf: at most one unit in the last place (exhaustively over
-// [1, 4), so over every binade), equal on 83% of inputs, exact at zero and
-// on subnormals.  The argument is a sum of squares, never negative.
+// [1, 4), so over every binade), equal on 83% of inputs, exact at zero.  The
+// flush-to-zero form drops the subnormal fix-up: a sum of squares below
+// 1.2e-38 (never negative) gives 0 instead of a value below 1.1e-19.
 __device__ __forceinline__ float amp_of(float2 v) {
     const float s = fmaf(v.x, v.x, v.y * v.y);
     float r;
-    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(s));
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
     return r;
 }
 
@@ -384,6 +385,7 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
     using G = ColsGeom<M>;
     constexpr int T = G::T, CS = G::CS, CP = G::CP, TWL = G::TWL;
     constexpr int PER = M / T;
+    static_assert((CP & (CP - 1)) == 0 && T % 2 == 0, "column pairs per CTA: a power of two");
 
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
@@ -473,6 +475,7 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
         const float2 *zp = (o == 0) ? ((kx == 0) ? a : pa) : pa;
         const int kxx = (o == 0) ? kx : N / 2;
         const float2 bx = __ldg(P.box_x + kxx);
+        const bool flip = ((kxx + lane) & 1) != 0;   // (-1)^(kx+ky): ky = lane + T*m, T even
 #pragma unroll
         for (int m = 0; m < PER; m++) {
             const int ky = lane + T * m;
@@ -486,7 +489,7 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
             A2.x -= m2 * bm.x;
             A2.y -= m2 * bm.y;
             float2 pr = cmulf_conj(A1, A2);
-            if ((kxx + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
+            if (flip) { pr.x = -pr.x; pr.y = -pr.y; }
             z[m] = pr;
         }
         float2 *dst = (o == 0) ? a : pa;
@@ -498,12 +501,14 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
     }
     __syncthreads();
     // write rows y in [ysearch, ysearch+nyc) of the half spectrum, kx <= N/2
-    const int nslots = CP + (b == 0 ? 1 : 0);
-    for (int i = threadIdx.x; i < nslots * P.nyc; i += blockDim.x) {
-        const int s = i % nslots, yq = i / nslots;
-        const int kxo = (s < CP) ? kx0 + s : N / 2;
-        P.qspec[((size_t)w * P.nyc + yq) * P.qpitch + kxo] = cols[s * CS + fft_pad(yq + P.ysearch)];
+    float2 *qw = P.qspec + (size_t)w * P.nyc * P.qpitch;
+    for (int i = threadIdx.x; i < CP * P.nyc; i += blockDim.x) {
+        const int s = i % CP, yq = i / CP;       // CP is a power of two
+        qw[(size_t)yq * P.qpitch + kx0 + s] = cols[s * CS + fft_pad(yq + P.ysearch)];
     }
+    if (b == 0)                                   // column N/2, the kx = 0 team's partner slot
+        for (int yq = threadIdx.x; yq < P.nyc; yq += blockDim.x)
+            qw[(size_t)yq * P.qpitch + N / 2] = cols[CP * CS + fft_pad(yq + P.ysearch)];
 }
 
 // ---------------------------------------------------------------- k_peak
@@ -585,6 +590,10 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
             v[m] = (e <= N / 2) ? make_float2(q1.x - q2.y, q1.y + q2.x) : make_float2(q1.x + q2.y, q2.x - q1.y);
         }
         team_fft_reg<N, +1>(v, ex, tw, lane);
+        // surface sums: 16 values per lane and row pair in FP32, then double
+        // (GB300's FP64 pipe is a small fraction of its FP32 rate; the partial
+        // sums' rounding, ~1e-7 relative, is far below what the statistics need)
+        float fpart = 0.f, hpart = 0.f;
 #pragma unroll
         for (int m = 0; m < PER; m++) {
             const int xq = lane + T * m - P.nx_corr / 2;
@@ -596,10 +605,12 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
             const unsigned long long k1 = argmax_key(c1, e1), k2 = argmax_key(c2, e2);
             best = k1 > best ? k1 : best;
             best = k2 > best ? k2 : best;
-            fsum += (double)c1 + (double)c2;
-            if (!(e1 & 512u)) hsum += (double)c1;      // reduce6<double,1024> keeps local [0,512) and [1024,1536)
-            if (!(e2 & 512u)) hsum += (double)c2;
+            fpart += c1 + c2;
+            if (!(e1 & 512u)) hpart += c1;      // reduce6<double,1024> keeps local [0,512) and [1024,1536)
+            if (!(e2 & 512u)) hpart += c2;
         }
+        fsum += (double)fpart;
+        hsum += (double)hpart;
     }
     best = warp_max_u64(best);
     hsum = warp_sum_f64(hsum);
