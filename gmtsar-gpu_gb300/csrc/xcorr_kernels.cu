@@ -730,7 +730,8 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
     float *md = reinterpret_cast<float *>(smem_raw);                 // [n2y*n2x]
     float2 *tr = reinterpret_cast<float2 *>(md + 64);                // [n2y][nx2]
     float2 *kys = tr + n2y * nx2;                                    // [ny2][n2y]
-    unsigned long long *rk = reinterpret_cast<unsigned long long *>(kys + ny2 * n2y);
+    float2 *kxs = kys + ny2 * n2y;                                   // [n2x][nx2], transposed
+    unsigned long long *rk = reinterpret_cast<unsigned long long *>(kxs + nx2 * n2x);
     int *fl = reinterpret_cast<int *>(rk + 8);
 
     const int w = blockIdx.x;
@@ -756,49 +757,65 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
         md[t] = v;
     }
     for (int t = threadIdx.x; t < ny2 * n2y; t += blockDim.x) kys[t] = __ldg(P.ky + t);
+    for (int t = threadIdx.x; t < nx2 * n2x; t += blockDim.x) {
+        const int X = t / n2x, c = t - X * n2x;
+        kxs[c * nx2 + X] = __ldg(P.kx + t);
+    }
     __syncthreads();
     // row pass: tr[r][X] = sum_c md[r][c] * KX[X][c]
     for (int t = threadIdx.x; t < n2y * nx2; t += blockDim.x) {
         const int r = t / nx2, X = t - r * nx2;
         float2 s = make_float2(0.f, 0.f);
-        for (int c = 0; c < n2x; c++) {
-            const float2 k = __ldg(P.kx + X * n2x + c);
-            const float m = md[r * n2x + c];
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const float2 k = kxs[c * nx2 + X];
+            const float m = md[r * 8 + c];
             s.x = fmaf(m, k.x, s.x);
             s.y = fmaf(m, k.y, s.y);
         }
         tr[t] = s;
     }
     __syncthreads();
-    // column pass, real part only, and the argmax: a thread keeps one column X
-    // of the row-pass result in registers (n2y = 8 values) and walks the
-    // output rows Y, four at a time; a warp shares Y, so the KY reads broadcast
+    // column pass, real part only, and the argmax: a thread keeps two columns
+    // (X and X + nx2/2) of the row-pass result in registers (2 x n2y values)
+    // and walks the output rows Y, four at a time; a warp shares Y, so each
+    // KY read is one broadcast that feeds both columns
     unsigned long long best = 0ull;
-    const int tpr = nx2 < (int)blockDim.x ? nx2 : (int)blockDim.x;     // threads per output row
+    const int half = nx2 / 2;
+    const int tpr = half < (int)blockDim.x ? half : (int)blockDim.x;   // threads per output row
     const int rp = (int)blockDim.x / tpr;                               // rows in flight per pass
-    for (int X = threadIdx.x % tpr; X < nx2; X += tpr) {
-        float2 tc[8];
+    const float4 *ky4 = reinterpret_cast<const float4 *>(kys);          // two KY entries per load
+    for (int X = threadIdx.x % tpr; X < half; X += tpr) {
+        float2 tc[2][8];
 #pragma unroll
-        for (int r = 0; r < 8; r++) tc[r] = tr[r * nx2 + X];
+        for (int r = 0; r < 8; r++) { tc[0][r] = tr[r * nx2 + X]; tc[1][r] = tr[r * nx2 + X + half]; }
         for (int Y = threadIdx.x / tpr; Y < ny2; Y += 4 * rp) {
-            float re[4] = {0.f, 0.f, 0.f, 0.f};
+            float re[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const int yy = Y + j * rp;
                 if (yy >= ny2) break;
 #pragma unroll
-                for (int r = 0; r < 8; r++) {
-                    const float2 k = kys[yy * 8 + r];
-                    re[j] = fmaf(k.x, tc[r].x, re[j]);
-                    re[j] = fmaf(-k.y, tc[r].y, re[j]);
+                for (int r2 = 0; r2 < 4; r2++) {
+                    const float4 k = ky4[yy * 4 + r2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        re[h][j] = fmaf(k.x, tc[h][2 * r2].x, re[h][j]);
+                        re[h][j] = fmaf(-k.y, tc[h][2 * r2].y, re[h][j]);
+                        re[h][j] = fmaf(k.z, tc[h][2 * r2 + 1].x, re[h][j]);
+                        re[h][j] = fmaf(-k.w, tc[h][2 * r2 + 1].y, re[h][j]);
+                    }
                 }
             }
 #pragma unroll
             for (int j = 0; j < 4; j++) {
                 const int yy = Y + j * rp;
                 if (yy >= ny2) break;
-                const unsigned long long kk = argmax_key(re[j], (unsigned)(yy * nx2 + X));
-                best = kk > best ? kk : best;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const unsigned long long kk = argmax_key(re[h][j], (unsigned)(yy * nx2 + X + h * half));
+                    best = kk > best ? kk : best;
+                }
             }
         }
     }
@@ -913,7 +930,7 @@ static size_t peak_smem() {
 }
 static size_t subpix_smem(const Plan &P) {
     return 64 * sizeof(float) + (size_t)P.n2y * P.nx2 * sizeof(float2) + (size_t)P.ny2 * P.n2y * sizeof(float2) +
-           8 * sizeof(unsigned long long) + 16;
+           (size_t)P.nx2 * P.n2x * sizeof(float2) + 8 * sizeof(unsigned long long) + 16;
 }
 
 template <int N>
