@@ -160,12 +160,24 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     const int lane = l32 % T;
     const int tm = l32 / T;                             // team within the warp
     const int team = warp * TPW + tm;
-    char *tbase = reinterpret_cast<char *>(tw + TWS) + (size_t)team * (PADN * sizeof(float2) + 2 * N * sizeof(float));
+    // The teams of a warp touch their amplitude rows and first-level sums
+    // with the same instruction; team tm's copies sit GOFF*tm words further
+    // on, and its amplitude rows are stored with index bit 0 flipped when tm
+    // is odd, so both the stride-2 interleaved stores of the interpolation
+    // and the lane-order loads hit distinct banks across the warp.
+    constexpr int RBP = 32;                             // padding words per team / per patch
+    constexpr int GOFF = 32 / TPW;
+    char *tbase = reinterpret_cast<char *>(tw + TWS) + (size_t)team * (PADN * sizeof(float2) + (2 * N + RBP) * sizeof(float));
     float2 *ex = reinterpret_cast<float2 *>(tbase);
-    float *rb = reinterpret_cast<float *>(ex + PADN);    // [2][N] amplitudes in natural order
+    float *rb = reinterpret_cast<float *>(ex + PADN) + tm * GOFF;    // [2][N] amplitudes, index i at i ^ (tm & 1)
+    // i ^ (tm & 1) is i + 1 or i - 1 by the parity of i: one base pointer per
+    // parity keeps the offsets of the unrolled accesses immediate
+    const int rbx = tm & 1;
+    float *const rbE = rb + rbx, *const rbO = rb - rbx;   // even / odd indices
+    float *const rbL = (lane & 1) ? rbO : rbE;            // indices lane + T*m (T even)
     float *acc = reinterpret_cast<float *>(reinterpret_cast<char *>(tw + TWS) +
-                                           (size_t)(blockDim.x / T) * (PADN * sizeof(float2) + 2 * N * sizeof(float))) +
-                 (size_t)warp * 2 * ACC;                 // [2][ACC] first-level sums of the warp's chunk
+                                           (size_t)(blockDim.x / T) * (PADN * sizeof(float2) + (2 * N + RBP) * sizeof(float))) +
+                 (size_t)warp * 2 * (ACC + RBP);         // [2][ACC + RBP] first-level sums of the warp's chunk
 
     for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_row[i];
     if constexpr (HSHIFT)
@@ -226,12 +238,13 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
 
     // amplitudes of one patch row into rb (natural order of the kept fine samples)
     auto amp_row = [&](int pt, int r, const uint32_t *raw) {
-        float *row = rb + pt * N;
+        float *const rowE = rbE + pt * N, *const rowO = rbO + pt * N;
         float2 v[PER];
         to_complex(raw, v);
         if (LG == 0) {
+            float *const rowL = rbL + pt * N;
 #pragma unroll
-            for (int m = 0; m < PER; m++) row[lane + T * m] = hypotf(v[m].x, v[m].y);
+            for (int m = 0; m < PER; m++) rowL[lane + T * m] = hypotf(v[m].x, v[m].y);
             return;
         }
         // interpolated rows differ from the reference's cuFFT rows by rounding
@@ -239,8 +252,8 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         // where the samples are the input itself (ri == 1, bit-exact)
 #pragma unroll
         for (int m = KM0; m < KM1; m++) {        // phase-0 samples are the input
-            const int k = ((lane + T * m) << LG) - N / 2;
-            row[k] = amp_of(v[m]);
+            const int k = ((lane + T * m) << LG) - N / 2;     // even
+            rowE[k] = amp_of(v[m]);
         }
 #pragma unroll 1
         for (int p = 1; p < ri; p++) {
@@ -261,7 +274,7 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
 #pragma unroll
             for (int m = KM0; m < KM1; m++) {
                 const int k = ((lane + T * m) << LG) + p - N / 2;
-                row[k] = amp_of(v[m]);
+                ((p & 1) ? rowO : rowE)[k] = amp_of(v[m]);
             }
         }
     };
@@ -286,7 +299,7 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
         float *a1g = P.amp1 + ((size_t)w * npy + r) * N;
         const bool r2c = (r >= P.ysearch) && (r < P.ysearch + P.ny_corr);
         float *a2g = P.amp2c + ((size_t)w * P.ny_corr + (r - P.ysearch)) * P.nx_corr;
-        float *acc1 = acc + tm * N, *acc2 = acc + ACC + tm * N;
+        float *acc1 = acc + tm * (N + GOFF), *acc2 = acc + (ACC + RBP) + tm * (N + GOFF);
         float2 v[PER];
         // the slave mask's columns [xsearch, N - xsearch) (xsearch = N/4) and
         // the time-correlation window's [xsearch, xsearch + nx_corr) are both
@@ -296,7 +309,7 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
 #pragma unroll
             for (int m = 0; m < PER; m++) {
                 const int e = lane + T * m;
-                const float a1 = rb[e], a2 = rb[N + e];
+                const float a1 = rbL[e], a2 = rbL[N + e];
                 const bool cin = (m >= PER / 4) && (m < 3 * PER / 4);
                 const bool in = rin && cin;
                 v[m] = make_float2(a1, in ? a2 : 0.f);
@@ -325,7 +338,7 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     for (int pt = 0; pt < 2; pt++) {
         float a[ACC / 32];
 #pragma unroll
-        for (int q = 0; q < ACC / 32; q++) a[q] = acc[pt * ACC + l32 + 32 * q];
+        for (int q = 0; q < ACC / 32; q++) a[q] = acc[pt * (ACC + RBP) + l32 + 32 * q + (32 * q / N) * GOFF];
 #pragma unroll
         for (int s = ACC / 64; s >= 1; s >>= 1)
 #pragma unroll
@@ -913,8 +926,8 @@ static size_t rows_smem() {
     constexpr int ACC = (N >= 1024) ? 1024 : 512;
     const int teams = 128 / T;
     return fft_twiddle_len(N) * (N <= 256 ? 2 : 1) * sizeof(float2) +
-           (size_t)teams * (fft_padded_len(N) * sizeof(float2) + 2 * N * sizeof(float)) +
-           (size_t)(128 / 32) * 2 * ACC * sizeof(float);
+           (size_t)teams * (fft_padded_len(N) * sizeof(float2) + (2 * N + 32) * sizeof(float)) +
+           (size_t)(128 / 32) * 2 * (ACC + 32) * sizeof(float);
 }
 template <int M>
 static size_t cols_smem(int) {
