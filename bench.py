@@ -201,10 +201,15 @@ def run_frame(args):
     ctx.set_profiling(False)
     # end to end through the host entry point (2.5 GB of images in per call)
     pm, ps = torch.from_numpy(m).pin_memory(), torch.from_numpy(s).pin_memory()
-    ctx.correlate(pm.numpy(), ps.numpy(), locs, strip_len=100)
-    t1 = time.perf_counter()
-    ctx.correlate(pm.numpy(), ps.numpy(), locs, strip_len=100)
-    e2e_s = time.perf_counter() - t1
+    pmn, psn = pm.numpy(), ps.numpy()
+    ctx.correlate(pmn, psn, locs, strip_len=100)
+    e2e_runs = []
+    for _ in range(3):                           # median of three calls
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ctx.correlate(pmn, psn, locs, strip_len=100)
+        e2e_runs.append(time.perf_counter() - t1)
+    e2e_s = sorted(e2e_runs)[1]
     line = {"metric": "xcorr windows/s, full frame, 256^2 windows (512^2 FFT)", "value": args.steps * nwin / (ms / 1e3),
             "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
@@ -214,7 +219,7 @@ def run_frame(args):
             "kernel_ms_per_step": {n: st.kernel_ms[i] for i, n in enumerate(xg.KERNEL_NAMES)},
             "batches_per_step": st.batches,
             "e2e": {"value": nwin / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(m.nbytes + s.nbytes + locs.nbytes),
-                    "d2h_bytes_per_step": int(nwin * xg.RESULT_DTYPE.itemsize), "timer": "host wall clock"},
+                    "d2h_bytes_per_step": int(nwin * xg.RESULT_DTYPE.itemsize), "timer": "host wall clock, median of 3 calls"},
             "clocks": clk}
     print(json.dumps(line), flush=True)
 
