@@ -86,15 +86,60 @@ __host__ __device__ constexpr int bitrev_c(int i) {
     return r;
 }
 
+// tan(pi/8) = sqrt(2) - 1
+__device__ constexpr float kT1 = 0.414213562373095048802f;
+
+// a +- b * exp(DIR * 2*pi*i * M16 / 16) for a rotation that is not a
+// multiple of a quarter turn, factored as in the tangent (Linzer-Feig)
+// butterfly: b * (c + i s) = f * (b + i r b) with f the larger of |c|, |s|
+// (signed) and |r| <= 1, so the pair costs 2 + 4 fused operations instead of
+// a 4-operation rotation and 4 additions.
+template <int M16, int DIR>
+__device__ __forceinline__ void tan_butterfly(float2 &a, float2 &b) {
+    constexpr int m = ((M16 % 16) + 16) % 16;
+    constexpr int q = m & 3;                      // angle within a quadrant: q * pi/8 (q != 0)
+    constexpr int quad = m >> 2;
+    // the rotation in quadrant 0 is (cq, sq); quadrant k multiplies by i^k
+    constexpr float cq = (q == 1) ? kC1 : (q == 2) ? kR2 : kS1;
+    constexpr float sq = (q == 1) ? kS1 : (q == 2) ? kR2 : kC1;
+    constexpr float c = (quad == 0) ? cq : (quad == 1) ? -sq : (quad == 2) ? -cq : sq;
+    constexpr float s = DIR * ((quad == 0) ? sq : (quad == 1) ? cq : (quad == 2) ? -sq : -cq);
+    float2 u;
+    float f;
+    if constexpr (q == 2) {                       // |c| = |s|: r = s / c = +-1
+        f = c;
+        u = (s == c) ? make_float2(b.x - b.y, b.y + b.x) : make_float2(b.x + b.y, b.y - b.x);
+    } else if constexpr ((q == 1) == (quad == 0 || quad == 2)) {   // |c| > |s|: factor c, r = s / c
+        constexpr float r = ((s > 0.f) == (c > 0.f)) ? kT1 : -kT1;
+        f = c;
+        u = make_float2(fmaf(-r, b.y, b.x), fmaf(r, b.x, b.y));
+    } else {                                      // |s| > |c|: factor s, b (c + i s) = s (r b + i b), r = c / s
+        constexpr float r = ((s > 0.f) == (c > 0.f)) ? kT1 : -kT1;
+        f = s;
+        u = make_float2(fmaf(r, b.x, -b.y), fmaf(r, b.y, b.x));
+    }
+    const float2 a0 = a;
+    a = make_float2(fmaf(f, u.x, a0.x), fmaf(f, u.y, a0.y));
+    b = make_float2(fmaf(-f, u.x, a0.x), fmaf(-f, u.y, a0.y));
+}
+
 // One butterfly stage of length LEN inside an R-point register DFT.
 template <int R, int LEN, int DIR, int K>
 struct DftStage {
     static __device__ __forceinline__ void run(float2 *t, int i) {
         if constexpr (K < LEN / 2) {
-            float2 a = t[i + K];
-            float2 b = rot16<K * (16 / LEN), DIR>(t[i + K + LEN / 2]);
-            t[i + K] = make_float2(a.x + b.x, a.y + b.y);
-            t[i + K + LEN / 2] = make_float2(a.x - b.x, a.y - b.y);
+            constexpr int M16 = K * (16 / LEN);
+            if constexpr ((M16 & 3) == 0) {       // quarter turns: exact swaps and signs
+                float2 a = t[i + K];
+                float2 b = rot16<M16, DIR>(t[i + K + LEN / 2]);
+                t[i + K] = make_float2(a.x + b.x, a.y + b.y);
+                t[i + K + LEN / 2] = make_float2(a.x - b.x, a.y - b.y);
+            } else {
+                float2 a = t[i + K], b = t[i + K + LEN / 2];
+                tan_butterfly<M16, DIR>(a, b);
+                t[i + K] = a;
+                t[i + K + LEN / 2] = b;
+            }
             DftStage<R, LEN, DIR, K + 1>::run(t, i);
         }
     }
