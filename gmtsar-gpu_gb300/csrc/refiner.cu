@@ -12,7 +12,8 @@
 //              fixed-order reductions over the batch) -> k_ref_adam
 //   inference: k_ref_infer, BF16 weights and activations on the tensor cores
 //              (mma.sync m16n8k16, FP32 accumulation), conv+GELU fused with
-//              the activations in shared memory.
+//              the activations channel-last in shared memory, one CTA per
+//              window at a time.
 // Loss per sample: 0.5 r^2 + 0.5 stopgrad(r^2) exp(-s) + s.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -287,9 +288,30 @@ __global__ void k_ref_adam(RefPlan R, float lr, float b1, float b2, float eps, f
 
 // transposed FP32 copies for the training forward and BF16 copies for inference
 __global__ void k_ref_derive(RefPlan R) {
+    __nv_bfloat16 *wb = reinterpret_cast<__nv_bfloat16 *>(R.wpack);
+    float *ws = reinterpret_cast<float *>(R.wpack + INF_ROWS * INF_KS * 2);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < INF_ROWS * INF_KS; e += gridDim.x * blockDim.x) {
+        const int n = e / INF_KS, kk = e % INF_KS;
+        float v = 0.f;
+        if (kk < 288) {
+            const int hi = kk >> 5, lo = kk & 31;        // tap (or dense input position), input channel
+            const int base = (n < 32) ? RP_W2 + n * 288 : (n < 64) ? RP_W3 + (n - 32) * 288 : RP_F1 + (n - 64) * 288;
+            v = R.theta[base + lo * 9 + hi];
+        }
+        wb[e] = __float2bfloat16_rn(v);
+    }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < INF_SMALL; e += gridDim.x * blockDim.x) {
+        float v = 0.f;
+        if (e < 288) v = R.theta[RP_W1 + e];
+        else if (e < 320) v = R.theta[RP_B1 + e - 288];
+        else if (e < 352) v = R.theta[RP_B2 + e - 320];
+        else if (e < 384) v = R.theta[RP_B3 + e - 352];
+        else if (e < 448) v = R.theta[RP_C1 + e - 384];
+        else if (e < 643) v = R.theta[RP_F2 + e - 448];       // F2 (192) then c2 (3)
+        ws[e] = v;
+    }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < RP_N; i += gridDim.x * blockDim.x) {
         const float t = R.theta[i];
-        R.wbf[i] = __float2bfloat16_rn(t);
         if (i >= RP_W2 && i < RP_W2 + 9216) { const int e = i - RP_W2, c = e / 288, kk = e % 288; R.w2t[kk * 32 + c] = t; }
         if (i >= RP_W3 && i < RP_W3 + 9216) { const int e = i - RP_W3, c = e / 288, kk = e % 288; R.w3t[kk * 32 + c] = t; }
         if (i >= RP_F1 && i < RP_F1 + 18432) { const int e = i - RP_F1, o = e / 288, h = e % 288; R.f1t[h * 64 + o] = t; }
@@ -306,150 +328,153 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
                  : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
 
-// One 16-row tile of a GEMM with N = 8*NT columns and K = 288: acc[nt] +=
-// A(16 x 288) * B(288 x 8nt).  fetchA(row, kk) returns the bf16 element (0 for
-// padded rows); Bs is [n][288] bf16 in shared memory.
-template <int NT, class FA>
-__device__ __forceinline__ void tile_gemm_288(float (&acc)[NT][4], FA fetchA, const __nv_bfloat16 *Bs, int lane) {
+// Per-CTA shared memory of the inference kernel after the parameter pack:
+// the window's input (81 f32, padded to 84) and its activations, channel-last
+// with a padded channel stride INF_CS (conv1 out 7x7, conv2 out 5x5, conv3
+// out 3x3, BF16), then the dense layer's 64 outputs (f32).
+constexpr int INF_CS = 40;
+constexpr int INF_ACT_BYTES = 84 * 4 + (49 + 25 + 9) * INF_CS * 2 + 64 * 4;
+
+// One warp's share of a convolution or dense layer as m16n8k16 tiles: rows are
+// output positions (mt: 16-row tile), columns output channels (n-tiles nt0,
+// nt0 + 1), K = 288 walked tap by tap (k' = 32 tap + c_in).  a_row(m) is the
+// BF16 activation row of output position m's tap-0 input (nullptr: padding
+// row), step(tap) the offset of tap's input row from it; B rows are INF_KS apart.
+template <class ARow, class Step>
+__device__ __forceinline__ void warp_gemm_288(float (&acc)[2][4], ARow a_row, Step step, const __nv_bfloat16 *B,
+                                              int mt, int nt0, int lane) {
     const int g = lane >> 2, t = lane & 3;
-#pragma unroll 2
+    const __nv_bfloat16 *r0 = a_row(mt * 16 + g), *r1 = a_row(mt * 16 + g + 8);
+    const __nv_bfloat16 *b0p = B + (size_t)(nt0 * 8 + g) * INF_KS + 2 * t;
+    const __nv_bfloat16 *b1p = b0p + 8 * INF_KS;
+#pragma unroll 3
     for (int ks = 0; ks < 18; ks++) {
-        const int k0 = ks * 16 + 2 * t;
+        const int off = step(ks >> 1) + (ks & 1) * 16 + 2 * t;
         uint32_t a[4];
-        a[0] = pack2(fetchA(g, k0), fetchA(g, k0 + 1));
-        a[1] = pack2(fetchA(g + 8, k0), fetchA(g + 8, k0 + 1));
-        a[2] = pack2(fetchA(g, k0 + 8), fetchA(g, k0 + 9));
-        a[3] = pack2(fetchA(g + 8, k0 + 8), fetchA(g + 8, k0 + 9));
-#pragma unroll
-        for (int nt = 0; nt < NT; nt++) {
-            const __nv_bfloat16 *bp = Bs + (size_t)(nt * 8 + g) * 288 + k0;
-            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(bp);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(bp + 8);
-            mma_bf16(acc[nt], a, b0, b1);
-        }
+        a[0] = r0 ? *reinterpret_cast<const uint32_t *>(r0 + off) : 0u;
+        a[1] = r1 ? *reinterpret_cast<const uint32_t *>(r1 + off) : 0u;
+        a[2] = r0 ? *reinterpret_cast<const uint32_t *>(r0 + off + 8) : 0u;
+        a[3] = r1 ? *reinterpret_cast<const uint32_t *>(r1 + off + 8) : 0u;
+        const int k0 = ks * 16;
+        mma_bf16(acc[0], a, *reinterpret_cast<const uint32_t *>(b0p + k0), *reinterpret_cast<const uint32_t *>(b0p + k0 + 8));
+        mma_bf16(acc[1], a, *reinterpret_cast<const uint32_t *>(b1p + k0), *reinterpret_cast<const uint32_t *>(b1p + k0 + 8));
     }
 }
 
-// Each warp takes 4 windows at a time: conv1 on the SIMT pipes (K = 9), conv2,
-// conv3 and the dense 288 -> 64 layer as tensor-core tiles with bias + GELU
-// applied to the accumulators, the 64 -> 3 layer on SIMT.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem) : "memory");
+}
+
+// A CTA of four warps per window at a time (grid-stride over the windows):
+// conv1 on the SIMT pipes in FP32 (K = 9), conv2, conv3 and the dense
+// 288 -> 64 layer as tensor-core tiles with bias + GELU applied to the
+// accumulators, the 64 -> 3 layer as warp dot products.  With the
+// activations channel-last, each A-fragment element pair is one 32-bit load.
 __global__ void __launch_bounds__(128) k_ref_infer(RefPlan R, const float *__restrict__ feat, float *__restrict__ out, int n) {
     extern __shared__ __align__(16) unsigned char smc[];
-    __nv_bfloat16 *B2 = reinterpret_cast<__nv_bfloat16 *>(smc);    // W2 [32][288]
-    __nv_bfloat16 *B3 = B2 + 9216;                                  // W3 [32][288]
-    __nv_bfloat16 *BF = B3 + 9216;                                  // F1 [64][288]
-    float *small = reinterpret_cast<float *>(BF + 18432);            // W1 (288), b1, b2, b3 (96), c1 (64), F2 (192), c2 (3)
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char *wbase = reinterpret_cast<unsigned char *>(small + 648) + warp * WARP_INFER_BYTES;
-    float *x0 = reinterpret_cast<float *>(wbase);                               // [4][81]
-    __nv_bfloat16 *a1 = reinterpret_cast<__nv_bfloat16 *>(x0 + 4 * 84);        // [4][32][49]
-    __nv_bfloat16 *a2 = a1 + 4 * 32 * 49;                                       // [4][32][25]
-    __nv_bfloat16 *a3 = a2 + 4 * 32 * 25;                                       // [4][288]
-    float *g1 = reinterpret_cast<float *>(a3 + 4 * 288);                        // [4][64]
-    for (int i = threadIdx.x; i < 9216; i += blockDim.x) { B2[i] = R.wbf[RP_W2 + i]; B3[i] = R.wbf[RP_W3 + i]; }
-    for (int i = threadIdx.x; i < 18432; i += blockDim.x) BF[i] = R.wbf[RP_F1 + i];
-    for (int i = threadIdx.x; i < 288; i += blockDim.x) small[i] = R.theta[RP_W1 + i];
-    for (int i = threadIdx.x; i < 32; i += blockDim.x) {
-        small[288 + i] = R.theta[RP_B1 + i]; small[320 + i] = R.theta[RP_B2 + i]; small[352 + i] = R.theta[RP_B3 + i];
-    }
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) small[384 + i] = R.theta[RP_C1 + i];
-    for (int i = threadIdx.x; i < 195; i += blockDim.x) small[448 + i] = R.theta[RP_F2 + i];   // F2 then c2
-    __syncthreads();
+    const __nv_bfloat16 *B2 = reinterpret_cast<const __nv_bfloat16 *>(smc);    // [32][INF_KS]
+    const __nv_bfloat16 *B3 = B2 + 32 * INF_KS;
+    const __nv_bfloat16 *BF = B3 + 32 * INF_KS;                                 // [64][INF_KS]
+    const float *small = reinterpret_cast<const float *>(smc + INF_ROWS * INF_KS * 2);
+    float *x0 = const_cast<float *>(small) + INF_SMALL;                          // [84]
+    __nv_bfloat16 *a1 = reinterpret_cast<__nv_bfloat16 *>(x0 + 84);             // [49][INF_CS]
+    __nv_bfloat16 *a2 = a1 + 49 * INF_CS;                                       // [25][INF_CS]
+    __nv_bfloat16 *a3 = a2 + 25 * INF_CS;                                       // [9][INF_CS]
+    float *g1 = reinterpret_cast<float *>(a3 + 9 * INF_CS);                     // [64]
     const float *W1 = small, *b1 = small + 288, *b2 = small + 320, *b3 = small + 352, *c1 = small + 384;
     const float *F2 = small + 448, *c2 = small + 448 + 192;
+
+    // the parameter pack, 16 bytes per copy (no waits on flags: cp.async groups)
+    for (int i = threadIdx.x; i < INF_PACK_BYTES / 16; i += blockDim.x) cp_async16(smc + 16 * i, R.wpack + 16 * i);
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
-    const int ngroups = (n + 3) / 4;
-    for (int grp = blockIdx.x * 4 + warp; grp < ngroups; grp += gridDim.x * 4) {
-        const int s0 = grp * 4;
-        const int nw = min(4, n - s0);
-        for (int i = lane; i < 4 * 81; i += 32) {
-            const int wl = i / 81, e = i % 81;
-            x0[wl * 84 + e] = (wl < nw) ? feat[(size_t)(s0 + wl) * 81 + e] : 0.f;
+    for (int w = blockIdx.x; w < n; w += gridDim.x) {
+        if (threadIdx.x < 81) x0[threadIdx.x] = feat[(size_t)w * 81 + threadIdx.x];
+        __syncthreads();
+        // conv1 (FP32): lane = output channel, warps take positions in turn
+        for (int p = warp; p < 49; p += 4) {
+            const int i = p / 7, j = p % 7;
+            float y = b1[lane];
+#pragma unroll
+            for (int d = 0; d < 9; d++) y = fmaf(W1[lane * 9 + d], x0[(i + d / 3) * 9 + j + d % 3], y);
+            a1[p * INF_CS + lane] = __float2bfloat16_rn(gelu_f(y));
         }
-        __syncwarp();
-        // conv1: lane = channel
-        for (int wl = 0; wl < 4; wl++)
-            for (int p = 0; p < 49; p++) {
-                const int i = p / 7, j = p % 7;
-                float y = b1[lane];
-#pragma unroll
-                for (int d = 0; d < 9; d++) y = fmaf(W1[lane * 9 + d], x0[wl * 84 + (i + d / 3) * 9 + j + d % 3], y);
-                a1[(wl * 32 + lane) * 49 + p] = __float2bfloat16_rn(gelu_f(y));
-            }
-        __syncwarp();
-        // conv2: rows (window, position) = 100 in 7 tiles of 16
-        for (int mt = 0; mt < 7; mt++) {
-            float acc[4][4] = {};
-            auto fa = [&](int r, int kk) -> __nv_bfloat16 {
-                const int m = mt * 16 + r;
-                if (m >= 100) return __float2bfloat16_rn(0.f);
-                const int wl = m / 25, p = m % 25, k = kk / 9, d = kk % 9;
-                return a1[(wl * 32 + k) * 49 + (p / 5 + d / 3) * 7 + p % 5 + d % 3];
-            };
-            tile_gemm_288<4>(acc, fa, B2, lane);
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++)
-#pragma unroll
-                for (int h = 0; h < 4; h++) {
-                    const int m = mt * 16 + g + (h >> 1) * 8, ch = nt * 8 + 2 * t + (h & 1);
-                    if (m < 100) a2[((m / 25) * 32 + ch) * 25 + m % 25] = __float2bfloat16_rn(gelu_f(acc[nt][h] + b2[ch]));
-                }
-        }
-        __syncwarp();
-        // conv3: rows (window, position) = 36 in 3 tiles
-        for (int mt = 0; mt < 3; mt++) {
-            float acc[4][4] = {};
-            auto fa = [&](int r, int kk) -> __nv_bfloat16 {
-                const int m = mt * 16 + r;
-                if (m >= 36) return __float2bfloat16_rn(0.f);
-                const int wl = m / 9, p = m % 9, k = kk / 9, d = kk % 9;
-                return a2[(wl * 32 + k) * 25 + (p / 3 + d / 3) * 5 + p % 3 + d % 3];
-            };
-            tile_gemm_288<4>(acc, fa, B3, lane);
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++)
-#pragma unroll
-                for (int h = 0; h < 4; h++) {
-                    const int m = mt * 16 + g + (h >> 1) * 8, ch = nt * 8 + 2 * t + (h & 1);
-                    if (m < 36) a3[(m / 9) * 288 + ch * 9 + m % 9] = __float2bfloat16_rn(gelu_f(acc[nt][h] + b3[ch]));
-                }
-        }
-        __syncwarp();
-        // dense 288 -> 64: rows = 4 windows (padded to 16)
+        __syncthreads();
+        // conv2: 25 positions (2 row tiles) x 32 channels (4 n-tiles); warp: tile mt = warp/2, n-tiles 2 (warp%2) +0/1
         {
-            float acc[8][4] = {};
-            auto fa = [&](int r, int kk) -> __nv_bfloat16 {
-                return (r < 4) ? a3[r * 288 + kk] : __float2bfloat16_rn(0.f);
+            float acc[2][4] = {};
+            auto row = [&](int m) -> const __nv_bfloat16 * {
+                return (m < 25) ? a1 + ((m / 5) * 7 + m % 5) * INF_CS : nullptr;
             };
-            tile_gemm_288<8>(acc, fa, BF, lane);
+            auto step = [&](int tap) { return ((tap / 3) * 7 + tap % 3) * INF_CS; };
+            const int mt = warp >> 1, nt0 = 2 * (warp & 1);
+            warp_gemm_288(acc, row, step, B2, mt, nt0, lane);
 #pragma unroll
-            for (int nt = 0; nt < 8; nt++)
+            for (int q = 0; q < 2; q++)
 #pragma unroll
                 for (int h = 0; h < 4; h++) {
-                    const int m = g + (h >> 1) * 8, o = nt * 8 + 2 * t + (h & 1);
-                    if (m < 4) g1[m * 64 + o] = gelu_f(acc[nt][h] + c1[o]);
+                    const int m = mt * 16 + g + (h >> 1) * 8, ch = (nt0 + q) * 8 + 2 * t + (h & 1);
+                    if (m < 25) a2[m * INF_CS + ch] = __float2bfloat16_rn(gelu_f(acc[q][h] + b2[ch]));
                 }
         }
-        __syncwarp();
-        if (lane < 12) {
-            const int wl = lane / 3, o = lane % 3;
-            float v = c2[o];
-            for (int k = 0; k < 64; k++) v = fmaf(F2[o * 64 + k], g1[wl * 64 + k], v);
-            if (wl < nw) out[(size_t)(s0 + wl) * 3 + o] = v;
+        __syncthreads();
+        // conv3: 9 positions (1 row tile) x 32 channels; warps 0, 1 take two n-tiles each
+        if (warp < 2) {
+            float acc[2][4] = {};
+            auto row = [&](int m) -> const __nv_bfloat16 * {
+                return (m < 9) ? a2 + ((m / 3) * 5 + m % 3) * INF_CS : nullptr;
+            };
+            auto step = [&](int tap) { return ((tap / 3) * 5 + tap % 3) * INF_CS; };
+            const int nt0 = 2 * warp;
+            warp_gemm_288(acc, row, step, B3, 0, nt0, lane);
+#pragma unroll
+            for (int q = 0; q < 2; q++)
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int m = g + (h >> 1) * 8, ch = (nt0 + q) * 8 + 2 * t + (h & 1);
+                    if (m < 9) a3[m * INF_CS + ch] = __float2bfloat16_rn(gelu_f(acc[q][h] + b3[ch]));
+                }
         }
-        __syncwarp();
+        __syncthreads();
+        // dense 288 -> 64: one row (this window), k' = 32 position + channel; warp: n-tiles 2 warp +0/1
+        {
+            float acc[2][4] = {};
+            auto row = [&](int m) -> const __nv_bfloat16 * { return (m == 0) ? a3 : nullptr; };
+            auto step = [&](int pos) { return pos * INF_CS; };
+            const int nt0 = 2 * warp;
+            warp_gemm_288(acc, row, step, BF, 0, nt0, lane);
+            if (g == 0)
+#pragma unroll
+                for (int q = 0; q < 2; q++)
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int o = (nt0 + q) * 8 + 2 * t + h;
+                        g1[o] = gelu_f(acc[q][h] + c1[o]);
+                    }
+        }
+        __syncthreads();
+        // 64 -> 3
+        if (warp == 0) {
+#pragma unroll
+            for (int o = 0; o < 3; o++) {
+                float v = fmaf(F2[o * 64 + lane], g1[lane], F2[o * 64 + 32 + lane] * g1[32 + lane]);
+#pragma unroll
+                for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+                if (lane == 0) out[(size_t)w * 3 + o] = v + c2[o];
+            }
+        }
+        __syncthreads();                           // x0 .. g1 are reused by the next window
     }
 }
 
 size_t ref_fwd_smem() { return (size_t)(2 * 9216 + 4 * 2816) * sizeof(float); }
 size_t ref_bwd_smem() { return (size_t)(2 * 9216 + 4 * 1184) * sizeof(float); }
-size_t ref_infer_smem() {
-    return (size_t)(9216 * 2 + 18432) * sizeof(__nv_bfloat16) + 648 * sizeof(float) + 4 * (size_t)WARP_INFER_BYTES;
-}
+size_t ref_infer_smem() { return (size_t)INF_PACK_BYTES + INF_ACT_BYTES; }
 
 cudaError_t ref_setup() {
     cudaError_t e = cudaFuncSetAttribute(k_ref_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ref_fwd_smem());
@@ -476,8 +501,8 @@ void ref_launch_adam(const RefPlan &R, float lr, int step, cudaStream_t s) {
 }
 void ref_launch_derive(const RefPlan &R, cudaStream_t s) { k_ref_derive<<<(RP_N + 255) / 256, 256, 0, s>>>(R); }
 void ref_launch_infer(const RefPlan &R, const float *feat, float *out, int n, cudaStream_t s) {
-    const int groups = (n + 3) / 4;
-    const int blocks = (groups + 3) / 4 < 456 ? (groups + 3) / 4 : 456;
+    // one window per CTA at a time, two CTAs per SM (84 KB of shared memory each)
+    const int blocks = n < 2 * 152 ? n : 2 * 152;
     k_ref_infer<<<blocks > 0 ? blocks : 1, 128, ref_infer_smem(), s>>>(R, feat, out, n);
 }
 

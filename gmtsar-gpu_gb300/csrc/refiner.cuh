@@ -11,14 +11,21 @@ constexpr int RP_W1 = 0, RP_B1 = 288, RP_W2 = 320, RP_B2 = 9536, RP_W3 = 9568, R
 // per-sample activation record (and the same layout for its gradients)
 constexpr int ACT_Y1 = 0, ACT_A1 = 1568, ACT_Y2 = 3136, ACT_A2 = 3936, ACT_Y3 = 4736, ACT_A3 = 5024, ACT_Z1 = 5312,
               ACT_G1 = 5376, ACT_OUT = 5440, REF_ACT = 5444;
-// shared bytes per warp in the inference kernel: x0 4x84 f32, a1 4x32x49 bf16,
-// a2 4x32x25 bf16, a3 4x288 bf16, g1 4x64 f32
-constexpr int WARP_INFER_BYTES = 4 * 84 * 4 + 4 * 32 * 49 * 2 + 4 * 32 * 25 * 2 + 4 * 288 * 2 + 4 * 64 * 4;
+// Inference parameter pack (built by k_ref_derive, copied whole into each
+// inference CTA's shared memory): 128 BF16 weight rows -- conv2 (32), conv3
+// (32), dense 288->64 (64) -- with K reordered tap- (or position-) major,
+// k' = 32 * tap + c_in, and padded to INF_KS so the B-fragment loads of
+// eight rows hit distinct banks; then INF_SMALL floats: conv1 weights (288),
+// biases b1 b2 b3 (3 x 32), dense bias c1 (64), the 64->3 layer (192 + 3).
+constexpr int INF_KS = 296;
+constexpr int INF_ROWS = 128;
+constexpr int INF_SMALL = 648;
+constexpr int INF_PACK_BYTES = INF_ROWS * INF_KS * 2 + INF_SMALL * 4;     // 78,368
 
 struct RefPlan {
     float *theta, *m, *v, *grad;        // RP_N each
     float *w2t, *w3t, *f1t;             // transposed FP32 copies (training forward)
-    __nv_bfloat16 *wbf;                 // BF16 copy (inference)
+    unsigned char *wpack;               // INF_PACK_BYTES, the inference parameter pack
     float *act, *grad_act;              // [batch][REF_ACT]
     float *loss;                        // [batch] per-sample loss (nullable)
     float *out;                         // [batch][3] training-forward outputs (nullable)

@@ -49,7 +49,7 @@ xcg_status xcg_refiner_create(int32_t device, int32_t max_batch, xcg_refiner **o
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += a256(bytes); return o; };
     const size_t o_th = take(np * 4), o_m = take(np * 4), o_v = take(np * 4), o_g = take(np * 4);
-    const size_t o_w2t = take(9216 * 4), o_w3t = take(9216 * 4), o_f1t = take(18432 * 4), o_bf = take(np * 2);
+    const size_t o_w2t = take(9216 * 4), o_w3t = take(9216 * 4), o_f1t = take(18432 * 4), o_bf = take(xcg::INF_PACK_BYTES);
     const size_t o_act = take((size_t)max_batch * xcg::REF_ACT * 4), o_gact = take((size_t)max_batch * xcg::REF_ACT * 4);
     const size_t o_loss = take((size_t)max_batch * 4), o_out = take((size_t)max_batch * 12);
     xcg_status st = ck(cudaMalloc(&r->mem, off), "cudaMalloc refiner");
@@ -57,7 +57,7 @@ xcg_status xcg_refiner_create(int32_t device, int32_t max_batch, xcg_refiner **o
     char *b = (char *)r->mem;
     r->R.theta = (float *)(b + o_th); r->R.m = (float *)(b + o_m); r->R.v = (float *)(b + o_v); r->R.grad = (float *)(b + o_g);
     r->R.w2t = (float *)(b + o_w2t); r->R.w3t = (float *)(b + o_w3t); r->R.f1t = (float *)(b + o_f1t);
-    r->R.wbf = (__nv_bfloat16 *)(b + o_bf);
+    r->R.wpack = (unsigned char *)(b + o_bf);
     r->R.act = (float *)(b + o_act); r->R.grad_act = (float *)(b + o_gact);
     r->R.loss = (float *)(b + o_loss);
     r->out_int = (float *)(b + o_out);
