@@ -705,7 +705,9 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
             for (int t = threadIdx.x; t < 81; t += NT) {
                 const int yy = ip - 4 + t / 9, xx = jp - 4 + t % 9;
                 float v = 0.f;
-                if (cmax > 0.0 && yy >= 0 && yy < nyc && xx >= 0 && xx < nxc) v = (float)((double)surf[yy * nxc + xx] / cmax);
+                // cmax is a float value: the FP32 quotient is the correctly rounded
+                // one, without the FP64 division (slow on GB300)
+                if (cmax > 0.0 && yy >= 0 && yy < nyc && xx >= 0 && xx < nxc) v = surf[yy * nxc + xx] / (float)cmax;
                 pd.feat[(size_t)local * 81 + t] = v;
             }
         }
