@@ -608,7 +608,12 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     P.winref = nullptr;
     P.locs = c->d_locs;
     xcg_status st = xcg::ctx_launch(c, P, bounds.data(), nb, s, rows_hook);
-    if (st != XCG_OK) return st;
+    if (st != XCG_OK) {
+        // band copies already queued read the caller's images: let them end
+        // before the caller may free those buffers
+        cudaStreamSynchronize(c->copy_stream);
+        return st;
+    }
     XCG_CK(cudaMemcpyAsync(h_res, c->d_res, (size_t)nlocs * sizeof(xcg_result), cudaMemcpyDeviceToHost, s), "copy results");
     XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     if (c->base.tc_form && c->tc_err) {     // a tensor-core wait that ran out leaves its block unwritten
