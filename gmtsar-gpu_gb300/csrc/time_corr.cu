@@ -12,8 +12,10 @@
 //   k_tcorr  per (lag tile, window): the master/slave ints are staged in
 //            shared memory by bands of window rows; each thread keeps 2 x 4
 //            lags in registers and slides along the window row, so one
-//            shared load feeds 8 multiply-adds per sum.  Sums are 64-bit
-//            (time: exact; time4: modulo 2^64 like the reference's long long).
+//            shared load feeds 8 multiply-adds of the cross sum; the master
+//            energy of every lag comes from sliding window sums.  Sums are
+//            64-bit (time: exact; time4: modulo 2^64 like the reference's
+//            long long).
 //   k_tpeak  per window: the scan-order peak, outputs, 8x8 neighbourhood.
 #include <cuda_runtime.h>
 #include <math.h>
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_tcorr(Plan P) {
 #pragma unroll
     for (int a = 0; a < RI; a++)
 #pragma unroll
-        for (int b = 0; b < RJ; b++) { sab[a][b] = 0; saa[a][b] = 0; }
+        for (int b = 0; b < RJ; b++) sab[a][b] = 0;
     S sbb = 0;
 
 #pragma unroll 1
@@ -163,10 +165,43 @@ __global__ void __launch_bounds__(TC_THREADS) k_tcorr(Plan P) {
 #pragma unroll
                 for (int a = 0; a < RI; a++)
 #pragma unroll
-                    for (int b = 0; b < RJ; b++) {
-                        sab[a][b] += Tr::prod(wa[a][b], bv);
-                        saa[a][b] += Tr::prod(wa[a][b], wa[a][b]);
-                    }
+                    for (int b = 0; b < RJ; b++) sab[a][b] += Tr::prod(wa[a][b], bv);
+            }
+        }
+        __syncthreads();
+    }
+    // Sums of a*a (time4: u*u) over each lag's master window, from sliding
+    // sums instead of a second multiply-add per lag and element (exact in
+    // 64 bits, or modulo 2^64 like the main sums): D[i][x] = the column sum
+    // over the window rows of lag row i, for the tile's AW columns, in the
+    // shared memory the bands used (it fits: TI * AW * 8 bytes).
+    {
+        S *D = reinterpret_cast<S *>(sb);
+        const int ar0 = P.ysearch + i0, ac0 = P.xsearch + j0;
+        auto sq = [&](int r, int cc) -> S {
+            const E e = Tr::elem(demeaned_int(amp1[(size_t)r * N + ac0 + cc], m1f));
+            return Tr::prod(e, e);
+        };
+        for (int x = threadIdx.x; x < AW; x += TC_THREADS) {
+            S d = 0;
+            for (int y = 0; y < ny_corr; y++) d += sq(ar0 + y, x);
+            D[x] = d;
+            for (int i = 1; i < TI; i++) {
+                d += sq(ar0 + i - 1 + ny_corr, x) - sq(ar0 + i - 1, x);
+                D[(size_t)i * AW + x] = d;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int a = 0; a < RI; a++) {
+            const S *drow = D + (size_t)(RI * ty + a) * AW + RJ * tx;
+            S e = 0;
+            for (int x = 0; x < nx_corr; x++) e += drow[x];
+            saa[a][0] = e;
+#pragma unroll
+            for (int b = 1; b < RJ; b++) {
+                e += drow[nx_corr + b - 1] - drow[b - 1];
+                saa[a][b] = e;
             }
         }
         __syncthreads();
