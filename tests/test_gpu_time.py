@@ -72,3 +72,17 @@ def test_time_mode_rejected_where_unsupported():
                                     buf.data_ptr())
     with pytest.raises(xg.XcgError):
         xg.Stack(p)
+
+
+@pytest.mark.parametrize("xs,ys", [(64, 64), (128, 32)])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_time_modes_larger_windows(xs, ys, mode):
+    """Wider lag tiles and windows than the golden cases (nx_corr 128 and
+    256: the master-energy sliding sums span 191 and 319 columns)."""
+    nx, ny = 8 * xs, 8 * ys
+    m, s = synth.make_pair(PairSpec(nx=nx, ny=ny, dx=-1.6, dy=2.3, noise_frac=0.05, seed=xs + ys + mode))
+    locs = xg.grid(nx, ny, 2, 2, xs, ys)
+    with xg.Context(xg.params(xs, ys, corr_mode=mode)) as ctx:
+        r = ctx.correlate(m, s, locs, strip_len=2)
+    o = xo.run(xo.params(xs, ys, corr_mode=mode), m, s, locs, precision=xo.F32, strip_len=2)
+    _compare(r, o, min_same=1.0, mode=mode)
