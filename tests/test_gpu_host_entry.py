@@ -70,3 +70,16 @@ def test_single_strip_job(pairs):
         r = ctx.correlate(m1, s1, locs, strip_len=6)
         d = _device(ctx, m1, s1, locs, 6)
     _same(r, d)
+
+
+def test_real_format_rows():
+    """float32 real samples (-real): one 32-bit word per sample, like the
+    int16 I/Q pairs, so the same row bands apply."""
+    m, s = synth.make_pair(synth.PairSpec(nx=1024, ny=2048, dx=1.1, dy=-0.7, noise_frac=0.1, seed=23, real=True))
+    locs = xg.grid(1024, 2048, 6, 20, 64, 64)
+    part = locs[(locs[:, 1] > 500) & (locs[:, 1] < 1500)]
+    p = xg.params(64, 64, fmt=1)
+    with xg.Context(p, max_batch=48) as ctx:
+        r = ctx.correlate(m, s, part, strip_len=6)
+        d = _device(ctx, m, s, part, 6)
+    _same(r, d)
