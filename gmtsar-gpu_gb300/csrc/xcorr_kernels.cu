@@ -489,11 +489,16 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
         const int kxx = (o == 0) ? kx : N / 2;
         const float2 bx = __ldg(P.box_x + kxx);
         const bool flip = ((kxx + lane) & 1) != 0;   // (-1)^(kx+ky): ky = lane + T*m, T even
+        // mirrored row M - ky: for m >= 1 it never wraps, and with T a multiple
+        // of 16 its padded index falls by T + T/16 per m (immediate offsets)
+        const float2 *zp1 = zp + fft_pad((M - lane - T) & (M - 1));
 #pragma unroll
         for (int m = 0; m < PER; m++) {
             const int ky = lane + T * m;
             const float2 z1 = zs[fft_pad(ky)];
-            const float2 z2 = zp[fft_pad((M - ky) & (M - 1))];
+            float2 z2;
+            if constexpr (T % 16 == 0) z2 = (m == 0) ? zp[fft_pad((M - lane) & (M - 1))] : zp1[-(m - 1) * (T + T / 16)];
+            else z2 = zp[fft_pad((M - ky) & (M - 1))];
             // A1 = (z1 + conj z2)/2, A2 = (z1 - conj z2)/(2i)
             float2 A1 = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
             float2 A2 = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
@@ -508,20 +513,29 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
         float2 *dst = (o == 0) ? a : pa;
         __syncwarp();                            // every lane has read a and pa before dst is reused
         team_fft_reg<M, +1>(z, dst, tw, lane);
+        // only the surface rows [ysearch, ysearch + nyc) = [M/4, 3M/4) go out
 #pragma unroll
-        for (int m = 0; m < PER; m++) dst[fft_pad(lane + T * m)] = z[m];
+        for (int m = PER / 4; m < 3 * PER / 4; m++) dst[fft_pad(lane + T * m)] = z[m];
         __syncwarp();
     }
     __syncthreads();
-    // write rows y in [ysearch, ysearch+nyc) of the half spectrum, kx <= N/2
-    float2 *qw = P.qspec + (size_t)w * P.nyc * P.qpitch;
-    for (int i = threadIdx.x; i < CP * P.nyc; i += blockDim.x) {
-        const int s = i % CP, yq = i / CP;       // CP is a power of two
-        qw[(size_t)yq * P.qpitch + kx0 + s] = cols[s * CS + fft_pad(yq + P.ysearch)];
+    // write rows y in [ysearch, ysearch+nyc) of the half spectrum, kx <= N/2:
+    // thread -> slot threadIdx % CP, rows threadIdx / CP + k * RS
+    {
+        constexpr int RS = G::THREADS / CP;        // = T
+        float2 *qw = P.qspec + (size_t)w * P.nyc * P.qpitch;
+        const int s = threadIdx.x % CP, y0 = threadIdx.x / CP;
+        float2 *dstq = qw + (size_t)y0 * P.qpitch + kx0 + s;
+        const float2 *srcc = cols + s * CS;
+        for (int k = 0; k < (M / 2) / RS; k++) {
+            // RS a multiple of 16: the padded row index steps by RS + RS/16
+            const int sy = (RS % 16 == 0) ? fft_pad(y0 + M / 4) + k * (RS + RS / 16) : fft_pad(y0 + M / 4 + k * RS);
+            dstq[(size_t)k * RS * P.qpitch] = srcc[sy];
+        }
+        if (b == 0)                                // column N/2, the kx = 0 team's partner slot
+            for (int yq = threadIdx.x; yq < M / 2; yq += blockDim.x)
+                qw[(size_t)yq * P.qpitch + N / 2] = cols[CP * CS + fft_pad(yq + M / 4)];
     }
-    if (b == 0)                                   // column N/2, the kx = 0 team's partner slot
-        for (int yq = threadIdx.x; yq < P.nyc; yq += blockDim.x)
-            qw[(size_t)yq * P.qpitch + N / 2] = cols[CP * CS + fft_pad(yq + P.ysearch)];
 }
 
 // ---------------------------------------------------------------- k_peak
