@@ -115,8 +115,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_tcorr(Plan P) {
         s1 = warp_sum_d(s1);
         s2 = warp_sum_d(s2);
         if (l32 == 0) {
-            s1 /= (double)(N * P.npy);
-            s2 /= (double)(N * P.npy);
+            const double inv = __longlong_as_double((long long)(1023 - (31 - __clz(N * P.npy))) << 52);   // 1/(N npy), a power of two
+            s1 *= inv;
+            s2 *= inv;
             mean_sh[0] = s1; mean_sh[1] = s2;
             if (blockIdx.x == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
         }

@@ -114,6 +114,12 @@ __device__ __forceinline__ float amp_of(float2 v) {
     return r;
 }
 
+// 1 / n for n a power of two, exactly (built from the exponent bits)
+__device__ __forceinline__ double pow2_inv(int n) {
+    const int lg = 31 - __clz(n);
+    return __longlong_as_double((long long)(1023 - lg) << 52);
+}
+
 __device__ __forceinline__ int slave_row_shift(const PairDev &pd, int y) {
     return (int)((double)y * pd.astretcha);    // ishft, read_xcorr_data.c:65
 }
@@ -403,7 +409,7 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *cols = tw + TWL;                   // [2*CP][CS]
-    double *sh = reinterpret_cast<double *>(cols + 2 * CP * CS);   // m1, m2
+    float *shf = reinterpret_cast<float *>(cols + 2 * CP * CS);    // m1 N M and m2 as floats
 
     const int w = blockIdx.y, b = blockIdx.x;
     const int N = P.npx;
@@ -447,16 +453,19 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
         s1 = warp_sum_f64(s1);
         s2 = warp_sum_f64(s2);
         if (l32 == 0) {
-            s1 /= (double)(N * M);
-            s2 /= (double)(N * M);
-            sh[0] = s1; sh[1] = s2;
+            // / (N M), a power of two: an exact scaling instead of an FP64 division
+            const double inv = pow2_inv(N * M);
+            s1 *= inv;
+            s2 *= inv;
+            shf[0] = (float)(s1 * (double)N * (double)M);   // the master's DC term, m1 N M
+            shf[1] = (float)s2;
             if (b == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
         }
     }
     cp_async_wait<1>();                          // partner columns in (this thread's copies)
     __syncthreads();                             // ... and everyone's
-    const float dc1 = (float)(sh[0] * (double)N * (double)M);
-    const float m2 = (float)sh[1];
+    const float dc1 = shf[0];
+    const float m2 = shf[1];
 
     const int kx = kx0 + team;
     float2 *a = cols + team * CS;
@@ -702,8 +711,9 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
         o.ip = ip; o.jp = jp;
         o.flags = (bc[3] != 0.0) ? XCG_FLAG_OOB : 0;
         o.cmax = cmax;
-        o.cave = rd[0] / (double)(nxc * nyc);
-        o.cave_true = rd[8] / (double)(nxc * nyc);
+        const double inv_ns = pow2_inv(nxc * nyc);      // exact: nxc * nyc is a power of two
+        o.cave = rd[0] * inv_ns;
+        o.cave_true = rd[8] * inv_ns;
         o.gamma = gamma;
         o.mean1 = P.means[2 * w];
         o.mean2 = P.means[2 * w + 1];
