@@ -196,8 +196,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_inv(Plan P) {
             s2 += __shfl_xor_sync(0xffffffffu, s2, o);
         }
         if (l32 == 0) {
-            s1 /= (double)(N * M);
-            s2 /= (double)(N * M);
+            // / (N M), a power of two: exact scaling instead of an FP64 division
+            const double inv = __longlong_as_double((long long)(1023 - (31 - __clz(N * M))) << 52);
+            s1 *= inv;
+            s2 *= inv;
             msh[0] = s1; msh[1] = s2;
             P.means[2 * w] = s1; P.means[2 * w + 1] = s2;
             // |A1|, |A2| <= 2 |Y|max after the mean corrections: |product| < (2 sqrt2 ymax)^2
