@@ -105,7 +105,16 @@ __device__ __forceinline__ unsigned *ymax_slot(const Plan &P, int w) {
     return reinterpret_cast<unsigned *>(P.surf + (size_t)w * P.nyc * P.nxc);
 }
 
-constexpr int TC_THREADS = 256;
+// warps per CTA of the precision-form stages: the MMA issuer, the A
+// producer and the rest producing the data operand.  The forward stages
+// convert plain loads (8 warps measured best); the inverse stage forms the
+// conjugate product from two spectrum reads per element first, and more
+// producer warps keep more of those loads in flight (16 warps: 0.48 -> 0.38
+// ms per 1000 windows).
+constexpr int TC_WARPS = 8;
+constexpr int TC_THREADS = 32 * TC_WARPS;
+constexpr int TC_WARPS_INV = 16;
+constexpr int TC_THREADS_INV = 32 * TC_WARPS_INV;
 // forward stages (512 accumulator columns): 16-wide K chunks, 4 stages (160 KB);
 // the inverse (up to 288 columns, fewer MMAs per chunk): 32-wide chunks, 4 stages
 constexpr int TC_STAGES = 4;
@@ -144,7 +153,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_rows(Plan P) {
 #pragma unroll
         for (int i = 0; i < 16; i++) base[((size_t)(r0 + n0 + i) * N + kx) * 2] = v[i] * (1.0f / S_ROW);
     };
-    tc::gemm_block_ws<2 * N / 128, 128, TC_STAGES, true>(P.tc_a_row, 2 * N, load, cvt, epi, P.tc_err);
+    tc::gemm_block_ws<2 * N / 128, 128, TC_STAGES, true, TC_KC, TC_WARPS>(P.tc_a_row, 2 * N, load, cvt, epi, P.tc_err);
 }
 
 template <int M>
@@ -164,7 +173,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_cols(Plan P) {
             ymax = fmaxf(ymax, fabsf(o));
         });
     };
-    tc::gemm_block_ws<2 * M / 128, 128, TC_STAGES, false>(P.tc_a_col, 2 * M, load, cvt, epi, P.tc_err);
+    tc::gemm_block_ws<2 * M / 128, 128, TC_STAGES, false, TC_KC, TC_WARPS>(P.tc_a_col, 2 * M, load, cvt, epi, P.tc_err);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ymax = fmaxf(ymax, __shfl_xor_sync(0xffffffffu, ymax, o));
     if ((threadIdx.x & 31) == 0) atomicMax(ymax_slot(P, w), __float_as_uint(ymax));
@@ -179,7 +188,7 @@ struct TcShapes {
 };
 
 template <int M>
-__global__ void __launch_bounds__(TC_THREADS, 1) k_tc_inv(Plan P) {
+__global__ void __launch_bounds__(TC_THREADS_INV, 1) k_tc_inv(Plan P) {
     const int N = P.npx;
     const int w = blockIdx.x;
     const float2 *z = P.zrow + (size_t)w * M * N;
@@ -245,8 +254,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_inv(Plan P) {
             if (n0 + col <= N / 2) q[((size_t)(yq0 + j) * P.qpitch + n0 + col) * 2 + c] = x / su;
         });
     };
-    tc::gemm_block_ws<TcShapes<M>::MT_INV, TcShapes<M>::NT_INV, TC_STAGES_INV, false, TC_KC_INV>(P.tc_a_inv, 2 * M, load,
-                                                                                                cvt, epi, P.tc_err);
+    tc::gemm_block_ws<TcShapes<M>::MT_INV, TcShapes<M>::NT_INV, TC_STAGES_INV, false, TC_KC_INV, TC_WARPS_INV>(
+        P.tc_a_inv, 2 * M, load, cvt, epi, P.tc_err);
 }
 
 // Real 2x2-block embedding of rows [row0, row0 + nrows) of an n-point DFT
@@ -341,7 +350,7 @@ static void launch_tc_t(const Plan &P, int stage, cudaStream_t s) {
     else if (stage == 1)
         k_tc_cols<n><<<dim3(n / 128, P.nwin), TC_THREADS, tc::WsGeom<S::MT_FWD, 128, TC_STAGES>::SMEM, s>>>(P);
     else
-        k_tc_inv<n><<<P.nwin, TC_THREADS, tc::WsGeom<S::MT_INV, S::NT_INV, TC_STAGES_INV, TC_KC_INV>::SMEM, s>>>(P);
+        k_tc_inv<n><<<P.nwin, TC_THREADS_INV, tc::WsGeom<S::MT_INV, S::NT_INV, TC_STAGES_INV, TC_KC_INV>::SMEM, s>>>(P);
 }
 void launch_tc_rows(const Plan &P, cudaStream_t s) { P.npx == 256 ? launch_tc_t<256>(P, 0, s) : launch_tc_t<128>(P, 0, s); }
 void launch_tc_cols(const Plan &P, cudaStream_t s) { P.npx == 256 ? launch_tc_t<256>(P, 1, s) : launch_tc_t<128>(P, 1, s); }

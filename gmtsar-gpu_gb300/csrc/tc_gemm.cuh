@@ -61,7 +61,7 @@ __host__ __device__ inline size_t prepared_bytes(int K) {
 //     full[c % NS] (one arrival per warp).
 // With NS = 4 the producers run up to four chunks ahead of the MMAs.  All
 // waits are bounded; a timeout raises *err and every role winds down.
-template <int MT, int NT, int NS, int KC_ = 16>
+template <int MT, int NT, int NS, int KC_ = 16, int NW = 8>
 struct WsGeom {
     static constexpr int KC = KC_;
     static constexpr uint32_t SBO = KC * 16u;
@@ -72,13 +72,14 @@ struct WsGeom {
     static constexpr uint32_t TMEM_COLS = TMEM_COLS_USED <= 32 ? 32 : TMEM_COLS_USED <= 64 ? 64
                                         : TMEM_COLS_USED <= 128 ? 128 : TMEM_COLS_USED <= 256 ? 256 : 512;
     static_assert(TMEM_COLS_USED <= 512 && NT % 16 == 0 && NT <= 256, "shape");
-    static constexpr int PRODUCERS = 192;            // warps 2..7
+    static_assert(NW >= 4 && NW % 4 == 0, "warps: a multiple of four (TMEM lane quarters)");
+    static constexpr int PRODUCERS = (NW - 2) * 32;  // warps 2 .. NW-1
     static constexpr size_t SMEM = (size_t)NS * STAGE + (2 * NS + 1) * 8 + 16;
 };
 
-template <int MT, int NT, int NS, bool K_FAST, int KC_ = 16, class Load, class Cvt, class Epi>
+template <int MT, int NT, int NS, bool K_FAST, int KC_ = 16, int NW = 8, class Load, class Cvt, class Epi>
 __device__ void gemm_block_ws(const uint8_t *__restrict__ a_prep, int K, Load load, Cvt cvt, Epi epi, int *err) {
-    using G = WsGeom<MT, NT, NS, KC_>;
+    using G = WsGeom<MT, NT, NS, KC_, NW>;
     constexpr int KC = G::KC;
     constexpr int PAIRS = NT * (KC / 2);
     constexpr int ITEMS = (PAIRS + G::PRODUCERS - 1) / G::PRODUCERS;
@@ -222,7 +223,7 @@ __device__ void gemm_block_ws(const uint8_t *__restrict__ a_prep, int K, Load lo
 #pragma unroll 1
         for (int t = 0; t < MT; t++) {
 #pragma unroll 1
-            for (int n0 = 16 * (warp >> 2); n0 < NT; n0 += 32) {
+            for (int n0 = 16 * (warp >> 2); n0 < NT; n0 += 16 * (NW / 4)) {
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(t * NT + n0), v);
                 epi(t * 128 + 32 * (warp & 3) + lane, n0, v);
