@@ -83,3 +83,27 @@ def test_real_format_rows():
         r = ctx.correlate(m, s, part, strip_len=6)
         d = _device(ctx, m, s, part, 6)
     _same(r, d)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_random_geometry(seed):
+    """Seeded random jobs: window size, strip length (ragged last strip),
+    location order by strip, slave offsets and azimuth stretch, batch size;
+    every result field bit-identical to the device entry."""
+    rng = np.random.default_rng(100 + seed)
+    xs = int(rng.choice([32, 64]))
+    nx, ny = int(rng.choice([768, 1024])), int(rng.choice([1536, 2048]))
+    m, s = synth.make_pair(synth.PairSpec(nx=nx, ny=ny, dx=float(rng.uniform(-3, 3)), dy=float(rng.uniform(-3, 3)),
+                                          noise_frac=0.1, seed=200 + seed))
+    nxl = int(rng.integers(3, 9))
+    locs = xg.grid(nx, ny, nxl, int(rng.integers(8, 20)), xs, xs)
+    locs = locs[: len(locs) - int(rng.integers(0, nxl))]                 # ragged last strip
+    nst = (len(locs) + nxl - 1) // nxl
+    order = rng.permutation(nst)
+    locs = np.concatenate([locs[k * nxl:(k + 1) * nxl] for k in order])
+    y_offset = int(rng.integers(-20, 21))
+    ast = float(rng.uniform(-2e-3, 2e-3))
+    with xg.Context(xg.params(xs, xs), max_batch=int(rng.integers(16, 120))) as ctx:
+        r = ctx.correlate(m, s, locs, 0, y_offset, ast, strip_len=nxl)
+        d = _device(ctx, m, s, locs, nxl, y_offset, ast)
+    _same(r, d)
