@@ -503,7 +503,7 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     if (m_nx <= 0 || m_ny <= 0 || s_nx <= 0 || s_ny <= 0) return XCG_ERR_ARG;
     if (nlocs == 0) return XCG_OK;
     XCG_CK(cudaSetDevice(c->device), "cudaSetDevice");
-    const size_t es = c->prm.format == 0 ? 4 : 4;   // int16 I/Q pair or float32
+    const size_t es = 4;     // bytes per sample: an int16 I/Q pair or a float32
     const size_t need[2] = {(size_t)m_nx * m_ny * es, (size_t)s_nx * s_ny * es};
     for (int i = 0; i < 2; i++) {
         if (need[i] > c->img_bytes[i]) {
