@@ -223,6 +223,11 @@ class Context:
         """Host arrays in, host results out.  master/slave: (ny, nx, 2) int16 or (ny, nx) float32."""
         master = np.ascontiguousarray(master)
         slave = np.ascontiguousarray(slave)
+        for name, a in (("master", master), ("slave", slave)):
+            if self.params.format == 0 and (a.dtype != np.int16 or a.ndim != 3 or a.shape[2] != 2):
+                raise ValueError(f"{name}: complex int16 images are (ny, nx, 2) int16 arrays, got {a.dtype} {a.shape}")
+            if self.params.format == 1 and (a.dtype != np.float32 or a.ndim != 2):
+                raise ValueError(f"{name}: -real images are (ny, nx) float32 arrays, got {a.dtype} {a.shape}")
         locs = np.ascontiguousarray(locs, dtype=np.int32).reshape(-1, 2)
         out = np.zeros(len(locs), dtype=RESULT_DTYPE)
         _check(self._L.xcg_correlate(self._h, master.ctypes.data, master.shape[1], master.shape[0],

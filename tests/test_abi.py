@@ -71,3 +71,17 @@ def test_grid_matches_get_locations():
     assert g.shape == (1000, 2)
     assert tuple(g[0]) == (256 + 2 * 72, 256 + 72)
     assert tuple(g[-1]) == (256 + 21 * 72, 256 + 50 * 72)
+
+
+def test_correlate_rejects_wrong_image_layout():
+    # the image checks run before the library is called (no GPU needed)
+    ctx = xg.Context.__new__(xg.Context)
+    ctx.params, ctx._h = xg.params(32, 32), None
+    locs = np.zeros((1, 2), np.int32)
+    with pytest.raises(ValueError):
+        ctx.correlate(np.zeros((8, 8), np.float32), np.zeros((8, 8), np.float32), locs)
+    with pytest.raises(ValueError):
+        ctx.correlate(np.zeros((8, 8, 2), np.int32), np.zeros((8, 8, 2), np.int16), locs)
+    ctx.params = xg.params(32, 32, fmt=1)
+    with pytest.raises(ValueError):
+        ctx.correlate(np.zeros((8, 8, 2), np.int16), np.zeros((8, 8, 2), np.int16), locs)
