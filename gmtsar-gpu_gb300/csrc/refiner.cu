@@ -335,6 +335,7 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
 // out 3x3, BF16), then the dense layer's 64 outputs (f32).
 constexpr int INF_CS = 40;
 constexpr int INF_ACT_BYTES = 84 * 4 + (49 + 25 + 9) * INF_CS * 2 + 64 * 4;
+constexpr int INF_GROUPS = 2;      // windows per CTA at a time (four warps each)
 
 // One warp's share of a convolution or dense layer as m16n8k16 tiles: rows are
 // output positions (mt: 16-row tile), columns output channels (n-tiles nt0,
@@ -372,13 +373,16 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 // 288 -> 64 layer as tensor-core tiles with bias + GELU applied to the
 // accumulators, the 64 -> 3 layer as warp dot products.  With the
 // activations channel-last, each A-fragment element pair is one 32-bit load.
-__global__ void __launch_bounds__(128) k_ref_infer(RefPlan R, const float *__restrict__ feat, float *__restrict__ out, int n) {
+__global__ void __launch_bounds__(128 * INF_GROUPS) k_ref_infer(RefPlan R, const float *__restrict__ feat,
+                                                                 float *__restrict__ out, int n) {
     extern __shared__ __align__(16) unsigned char smc[];
     const __nv_bfloat16 *B2 = reinterpret_cast<const __nv_bfloat16 *>(smc);    // [32][INF_KS]
     const __nv_bfloat16 *B3 = B2 + 32 * INF_KS;
     const __nv_bfloat16 *BF = B3 + 32 * INF_KS;                                 // [64][INF_KS]
     const float *small = reinterpret_cast<const float *>(smc + INF_ROWS * INF_KS * 2);
-    float *x0 = const_cast<float *>(small) + INF_SMALL;                          // [84]
+    // one group of four warps per window; each group has its own activations
+    const int grp = threadIdx.x >> 7, gt = threadIdx.x & 127;
+    float *x0 = reinterpret_cast<float *>(smc + INF_PACK_BYTES + (size_t)grp * INF_ACT_BYTES);   // [84]
     __nv_bfloat16 *a1 = reinterpret_cast<__nv_bfloat16 *>(x0 + 84);             // [49][INF_CS]
     __nv_bfloat16 *a2 = a1 + 49 * INF_CS;                                       // [25][INF_CS]
     __nv_bfloat16 *a3 = a2 + 25 * INF_CS;                                       // [9][INF_CS]
@@ -391,10 +395,14 @@ __global__ void __launch_bounds__(128) k_ref_infer(RefPlan R, const float *__res
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
 
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = gt >> 5, lane = threadIdx.x & 31;      // warp within the group
     const int g = lane >> 2, t = lane & 3;
-    for (int w = blockIdx.x; w < n; w += gridDim.x) {
-        if (threadIdx.x < 81) x0[threadIdx.x] = feat[(size_t)w * 81 + threadIdx.x];
+    // the groups of a CTA take windows base + grp; barriers stay CTA-wide, so
+    // a group without a window in the last round still takes part in them
+    for (int base = blockIdx.x * INF_GROUPS; base < n; base += gridDim.x * INF_GROUPS) {
+        const int w = base + grp;
+        const bool have = w < n;
+        if (gt < 81) x0[gt] = have ? feat[(size_t)w * 81 + gt] : 0.f;
         __syncthreads();
         // conv1 (FP32): lane = output channel, warps take positions in turn
         for (int p = warp; p < 49; p += 4) {
@@ -459,7 +467,7 @@ __global__ void __launch_bounds__(128) k_ref_infer(RefPlan R, const float *__res
         }
         __syncthreads();
         // 64 -> 3
-        if (warp == 0) {
+        if (warp == 0 && have) {
 #pragma unroll
             for (int o = 0; o < 3; o++) {
                 float v = fmaf(F2[o * 64 + lane], g1[lane], F2[o * 64 + 32 + lane] * g1[32 + lane]);
@@ -474,7 +482,7 @@ __global__ void __launch_bounds__(128) k_ref_infer(RefPlan R, const float *__res
 
 size_t ref_fwd_smem() { return (size_t)(2 * 9216 + 4 * 2816) * sizeof(float); }
 size_t ref_bwd_smem() { return (size_t)(2 * 9216 + 4 * 1184) * sizeof(float); }
-size_t ref_infer_smem() { return (size_t)INF_PACK_BYTES + INF_ACT_BYTES; }
+size_t ref_infer_smem() { return (size_t)INF_PACK_BYTES + (size_t)INF_GROUPS * INF_ACT_BYTES; }
 
 cudaError_t ref_setup() {
     cudaError_t e = cudaFuncSetAttribute(k_ref_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ref_fwd_smem());
@@ -501,9 +509,10 @@ void ref_launch_adam(const RefPlan &R, float lr, int step, cudaStream_t s) {
 }
 void ref_launch_derive(const RefPlan &R, cudaStream_t s) { k_ref_derive<<<(RP_N + 255) / 256, 256, 0, s>>>(R); }
 void ref_launch_infer(const RefPlan &R, const float *feat, float *out, int n, cudaStream_t s) {
-    // one window per CTA at a time, two CTAs per SM (84 KB of shared memory each)
-    const int blocks = n < 2 * 152 ? n : 2 * 152;
-    k_ref_infer<<<blocks > 0 ? blocks : 1, 128, ref_infer_smem(), s>>>(R, feat, out, n);
+    // INF_GROUPS windows per CTA at a time, two CTAs per SM (91 KB of shared memory each)
+    const int need = (n + INF_GROUPS - 1) / INF_GROUPS;
+    const int blocks = need < 2 * 152 ? need : 2 * 152;
+    k_ref_infer<<<blocks > 0 ? blocks : 1, 128 * INF_GROUPS, ref_infer_smem(), s>>>(R, feat, out, n);
 }
 
 }  // namespace xcg
