@@ -27,7 +27,7 @@ using cd = std::complex<double>;
 
 // windows per row-stage sub-launch of the host-buffer entry
 #ifndef XCG_ROW_SUB
-#define XCG_ROW_SUB 128
+#define XCG_ROW_SUB 192
 #endif
 
 namespace {
