@@ -26,3 +26,11 @@ def test_reference_arm_line():
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert isinstance(d["config"], dict) and "workload" in d["config"]
+
+
+def test_roofline_traffic_figure_is_readable():
+    # bench.py scales the committed k_rows capture's DRAM bytes to its launch
+    sys.path.insert(0, ROOT)
+    import bench
+    per_window = bench.read_traffic()
+    assert per_window is not None and 5e5 < per_window < 2e6, per_window
