@@ -191,6 +191,7 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *
     P.pairs = nullptr;
     P.winref = nullptr;
     cudaStream_t s = (cudaStream_t)stream;
+    XCG_TRY(xcg::tc_reset_status(c, s));
     for (int w0 = 0; w0 < nlocs; w0 += bw) {
         P.win0 = w0;
         P.nwin = (nlocs - w0 < bw) ? nlocs - w0 : bw;

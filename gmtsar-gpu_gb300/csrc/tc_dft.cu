@@ -328,6 +328,19 @@ static xcg_status tc_enable_t(xcg_ctx *c) {
     return XCG_OK;
 }
 
+xcg_status tc_reset_status(xcg_ctx *c, cudaStream_t s) {
+    if (!c->base.tc_form || !c->tc_err) return XCG_OK;
+    // 0xff bytes: a nonzero flag, as a stage whose wait ran out leaves it
+    const int v = c->inject_tc_timeout ? 0xff : 0;
+    c->inject_tc_timeout = 0;
+    const cudaError_t e = cudaMemsetAsync(c->tc_err, v, sizeof(int), s);
+    if (e != cudaSuccess) {
+        set_last_error(cudaGetErrorString(e));
+        return XCG_ERR_CUDA;
+    }
+    return XCG_OK;
+}
+
 xcg_status tc_enable(xcg_ctx *c) {
     Plan &B = c->base;
     if (B.npx != B.npy || (B.npx != 256 && B.npx != 128)) {
@@ -363,6 +376,10 @@ extern "C" xcg_status xcg_set_dft_form(xcg_ctx *c, int32_t form) {
     if (cudaSetDevice(c->device) != cudaSuccess) return XCG_ERR_CUDA;
     if (form == 0) { c->base.tc_form = 0; return XCG_OK; }
     return xcg::tc_enable(c);
+}
+
+extern "C" void xcg_debug_inject_stage_timeout(xcg_ctx *c) {
+    if (c) c->inject_tc_timeout = 1;
 }
 
 extern "C" xcg_status xcg_tc_gemm_check(int32_t m_tiles, int32_t n_tile, int32_t k, int32_t n_total,

@@ -429,6 +429,10 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     // from and joined back into s); profiling runs them in order on s so each
     // kernel's events time that kernel alone
     const bool fork = nb > 1 && c->nslots > 1 && !c->profiling;
+    if (tcf) {             // a timeout of an earlier call must not be reported by this one
+        const xcg_status rs = tc_reset_status(c, s);
+        if (rs != XCG_OK) return rs;
+    }
     if (fork) {
         XCG_CK(cudaEventRecord(c->ev_fork, s), "cudaEventRecord");
         for (int k = 0; k < c->nslots; k++) XCG_CK(cudaStreamWaitEvent(c->slot_stream[k], c->ev_fork, 0), "cudaStreamWaitEvent");

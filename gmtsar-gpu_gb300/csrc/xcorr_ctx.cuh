@@ -47,6 +47,7 @@ struct xcg_ctx {
     // precision form: prepared DFT operands and the tensor-core error flag
     uint8_t *tc_prep = nullptr;
     int *tc_err = nullptr;
+    int inject_tc_timeout = 0;    // xcg_debug_inject_stage_timeout: the next call sets the flag instead of clearing it
     // profiling
     int profiling = 0;
     std::vector<cudaEvent_t> events;
@@ -71,6 +72,9 @@ Plan rows_subrange(Plan P, int off, int n);
 void set_last_error(const char *msg);
 // precision form (tc_dft.cu)
 xcg_status tc_enable(xcg_ctx *c);
+// Queues the reset of the tensor-core error flag on s at the start of a call
+// in the precision form (or its setting, when a timeout was injected).
+xcg_status tc_reset_status(xcg_ctx *c, cudaStream_t s);
 void launch_tc_rows(const Plan &P, cudaStream_t s);
 void launch_tc_cols(const Plan &P, cudaStream_t s);
 void launch_tc_inv(const Plan &P, cudaStream_t s);

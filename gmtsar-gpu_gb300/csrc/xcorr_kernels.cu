@@ -710,6 +710,9 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
         o.corr = (float)gamma;
         o.ip = ip; o.jp = jp;
         o.flags = (bc[3] != 0.0) ? XCG_FLAG_OOB : 0;
+        // precision form: the tensor-core stages before this kernel raise the
+        // flag when a bounded wait ran out and left part of a spectrum unwritten
+        if (P.tc_form && P.tc_err && *reinterpret_cast<volatile const int *>(P.tc_err)) o.flags |= XCG_FLAG_STAGE_TIMEOUT;
         o.cmax = cmax;
         const double inv_ns = pow2_inv(nxc * nyc);      // exact: nxc * nyc is a power of two
         o.cave = rd[0] * inv_ns;

@@ -14,7 +14,9 @@
 // loaded on a device and every device that loads the library keeps it until
 // the process exits.  A call that needs more than that is refused with
 // XCG_ERR_TOO_LARGE.  Nothing in this file calls cudaMalloc, cudaFree or a
-// library routine that allocates.
+// library routine that allocates, and nothing copies from host memory: the
+// transform tables are computed by a small kernel straight into the array,
+// so every call is one run of kernels on the caller's stream.
 //
 // On the host the array's name is only a stand-in for the device object: its
 // device address is looked up with cudaGetSymbolAddress, once per device, on
@@ -23,14 +25,16 @@
 // made before any stream capture starts.
 //
 // All calls share the array and it keeps whatever the last call left there.
-// The kernels write every scratch element they later read, so nothing has to
-// be cleared; two calls that overlap on the GPU (different streams, or
-// different host threads) race on the array and must be serialised by the
-// caller.
+// Each call rewrites the tables, and the kernels write every scratch element
+// they later read, so nothing has to be cleared; two calls that overlap on
+// the GPU (different streams, or different host threads) race on the array
+// and must be serialised by the caller.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
+
+#include <atomic>
 
 #include "team_fft.cuh"
 #include "xcorr_gb300.h"
@@ -41,58 +45,129 @@ static __device__ __align__(256) unsigned char g_xcg_noalloc_scratch[XCG_NOALLOC
 namespace {
 
 constexpr int kMaxDevices = 64;
-void *s_scratch_addr[kMaxDevices];   // device address of the array, per device (set up once)
+// device address of the array, per device; written once per device (every
+// writer stores the same value, and the atomic makes concurrent first calls
+// from several host threads well defined)
+std::atomic<void *> s_scratch_addr[kMaxDevices];
 
-// host-side table staging; thread-local so concurrent host threads do not share it
-constexpr size_t kMaxTable = 32768;  // float2 entries, enough for npx/npy <= 1024, ri <= 8, factor <= 64
-thread_local float2 t_tables[kMaxTable];
 thread_local char t_msg[256];
 
 size_t a256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-// Stockham pass twiddles (same construction as the context's tables).
-size_t put_twiddles(float2 *dst, int n) {
-    size_t k0 = 0;
+// The seven tables of a plan, as entry offsets (float2) into the start of the
+// array, each on a 256-byte boundary, in the order of the Plan fields.
+enum { T_TWR, T_TWC, T_PH, T_BX, T_BY, T_KX, T_KY, T_N };
+struct TableSet {
+    int off[T_N], len[T_N];
+    int total;                 // entries up to the end of the last table
+    int npx, npy, ri, xs, ys, n2x, nx2, n2y, ny2;
+};
+
+// Entries put_row_phase writes for n-point rows and factor ri.
+int row_phase_len(int n, int ri) { return ri == 1 ? 1 : (ri == 2 && n <= 256) ? n : (ri - 1) * n; }
+
+TableSet table_set(int npx, int npy, int ri, int xs, int ys, int n2x, int nx2, int n2y, int ny2) {
+    TableSet t;
+    const int len[T_N] = {xcg::fft_twiddle_len(npx), xcg::fft_twiddle_len(npy), row_phase_len(npx, ri), npx, npy,
+                          nx2 * n2x, ny2 * n2y};
+    int o = 0;
+    for (int k = 0; k < T_N; k++) {
+        t.off[k] = o;
+        t.len[k] = len[k];
+        o = (o + len[k] + 31) & ~31;
+    }
+    t.total = o;
+    t.npx = npx; t.npy = npy; t.ri = ri; t.xs = xs; t.ys = ys;
+    t.n2x = n2x; t.nx2 = nx2; t.n2y = n2y; t.ny2 = ny2;
+    return t;
+}
+
+// Products and sums below are written with explicit rounding so that no
+// multiply-add is fused: each entry is the double value the host-side table
+// builders of the context (xcorr_api.cu, put_row_phase) compute, rounded to
+// float.
+__device__ double2 d_polar(double a) { return make_double2(cos(a), sin(a)); }
+__device__ double2 d_cmul(double2 x, double2 y) {
+    return make_double2(__dsub_rn(__dmul_rn(x.x, y.x), __dmul_rn(x.y, y.y)),
+                        __dadd_rn(__dmul_rn(x.x, y.y), __dmul_rn(x.y, y.x)));
+}
+
+// Stockham pass twiddle i of an n-point FFT ([pass >= 1][r-1][k], forward sign).
+__device__ float2 stockham_twiddle(int n, int i) {
     int ns = 1;
     for (int p = 0; p < xcg::fft_npasses(n); p++) {
         const int r = xcg::fft_radix(n, p);
-        if (p > 0)
-            for (int rr = 1; rr < r; rr++)
-                for (int k = 0; k < ns; k++) {
-                    const double a = -2.0 * M_PI * (double)k * rr / ((double)ns * r);
-                    dst[k0++] = make_float2((float)cos(a), (float)sin(a));
-                }
+        if (p > 0) {
+            const int seg = (r - 1) * ns;
+            if (i < seg) {
+                const int rr = i / ns + 1, k = i % ns;
+                const double a = -2.0 * M_PI * (double)k * rr / ((double)ns * r);
+                return make_float2((float)cos(a), (float)sin(a));
+            }
+            i -= seg;
+        }
         ns *= r;
     }
-    return k0;
+    return make_float2(0.f, 0.f);
 }
 
-size_t put_interp(float2 *dst, int n, int m) {
-    for (int X = 0; X < m; X++)
-        for (int c = 0; c < n; c++) {
-            double sr = 0.0, si = 0.0;
-            for (int f = 0; f < n; f++) {
-                const int fp = (f < n / 2) ? f : f - n;
-                const double a = -2.0 * M_PI * f * c / n + 2.0 * M_PI * fp * X / m;
-                sr += cos(a);
-                si += sin(a);
-            }
-            dst[(size_t)X * n + c] = make_float2((float)(sr / n), (float)(si / n));
-        }
-    return (size_t)m * n;
-}
-
-size_t put_box(float2 *dst, int n, int lo) {
-    for (int k = 0; k < n; k++) {
-        double sr = 0.0, si = 0.0;
-        for (int c = lo; c < n - lo; c++) {
-            const double a = -2.0 * M_PI * (double)k * c / n;
-            sr += cos(a);
-            si += sin(a);
-        }
-        dst[k] = make_float2((float)sr, (float)si);
+// Entry i of the row kernel's range-interpolation table (put_row_phase).
+__device__ float2 row_phase(int n, int ri, int i) {
+    if (ri == 1) return make_float2(0.f, 0.f);
+    if (ri == 2 && n <= 256) {
+        const int r = i / 16 + 1, k = i % 16;
+        if (r >= n / 16) return make_float2(0.f, 0.f);
+        const double a = -2.0 * M_PI * r * (k + 0.5) / n;
+        return make_float2((float)cos(a), (float)sin(a));
     }
-    return (size_t)n;
+    const int q = i / n + 1, f = i % n;
+    const int fp = (f < n / 2) ? f : f - n;
+    const double a = 2.0 * M_PI * fp * q / ((double)ri * n);
+    return make_float2((float)(cos(a) / n), (float)(sin(a) / n));
+}
+
+// DFT bin k of the 0/1 mask with ones on [lo, n - lo) (box_spectrum).
+__device__ float2 box_bin(int n, int lo, int k) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int c = lo; c < n - lo; c++) {
+        const double2 w = d_polar(-2.0 * M_PI * (double)k * c / n);
+        s.x = __dadd_rn(s.x, w.x);
+        s.y = __dadd_rn(s.y, w.y);
+    }
+    return make_float2((float)s.x, (float)s.y);
+}
+
+// Entry (X, c) of the zero-pad interpolation operator from n to m samples (interp_operator).
+__device__ float2 interp_entry(int n, int m, int i) {
+    const int X = i / n, c = i % n;
+    double2 s = make_double2(0.0, 0.0);
+    for (int f = 0; f < n; f++) {
+        const int fp = (f < n / 2) ? f : f - n;
+        const double2 v = d_cmul(d_polar(-2.0 * M_PI * f * c / n), d_polar(2.0 * M_PI * fp * X / m));
+        s.x = __dadd_rn(s.x, v.x);
+        s.y = __dadd_rn(s.y, v.y);
+    }
+    return make_float2((float)__ddiv_rn(s.x, (double)n), (float)__ddiv_rn(s.y, (double)n));
+}
+
+__global__ void k_noalloc_tables(TableSet t, float2 *dst) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < t.total; g += gridDim.x * blockDim.x) {
+        int k = T_N - 1;
+        while (k > 0 && g < t.off[k]) k--;
+        const int i = g - t.off[k];
+        if (i >= t.len[k]) continue;              // alignment gap
+        float2 v;
+        switch (k) {
+            case T_TWR: v = stockham_twiddle(t.npx, i); break;
+            case T_TWC: v = stockham_twiddle(t.npy, i); break;
+            case T_PH: v = row_phase(t.npx, t.ri, i); break;
+            case T_BX: v = box_bin(t.npx, t.xs, i); break;
+            case T_BY: v = box_bin(t.npy, t.ys, i); break;
+            case T_KX: v = interp_entry(t.n2x, t.nx2, i); break;
+            default: v = interp_entry(t.n2y, t.ny2, i); break;
+        }
+        dst[g] = v;
+    }
 }
 
 xcg_status fail(xcg_status st, const char *msg) {
@@ -132,16 +207,18 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return fail(XCG_ERR_NO_DEVICE, "no current device");
-    if (!s_scratch_addr[dev]) {        // once per device, with that device current
+    void *addr = s_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!addr) {        // once per device, with that device current
         void *ptr = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&ptr, g_xcg_noalloc_scratch);
         if (e != cudaSuccess || !ptr) {
             snprintf(t_msg, sizeof t_msg, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
             return fail_msg(XCG_ERR_CUDA);
         }
-        s_scratch_addr[dev] = ptr;
+        s_scratch_addr[dev].store(ptr, std::memory_order_release);
+        addr = ptr;
     }
-    char *base = (char *)s_scratch_addr[dev];
+    char *base = (char *)addr;
 
     xcg::Plan P;
     memset(&P, 0, sizeof P);
@@ -156,20 +233,13 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
     P.n2x = p->n2x; P.n2y = p->n2y;
     P.nx2 = P.n2x * P.ifc; P.ny2 = P.n2y * P.ifc;
     P.format = p->format;
+    P.corr_mode = 2;            // frequency domain, the only mode this entry runs
     P.nchunks = P.npx * P.npy / 1024;
     P.qpitch = P.npx / 2 + 16;
 
-    // tables into the thread-local staging buffer
-    size_t o = 0, o_twr, o_twc, o_ph, o_bx, o_by, o_kx, o_ky;
-    auto align = [&]() { o = (o + 31) & ~(size_t)31; };     // 256-byte boundaries
-    o_twr = o; o += put_twiddles(t_tables + o, P.npx); align();
-    o_twc = o; o += put_twiddles(t_tables + o, P.npy); align();
-    o_ph = o; o += xcg::put_row_phase(t_tables + o, P.npx, P.ri); align();
-    o_bx = o; o += put_box(t_tables + o, P.npx, xs); align();
-    o_by = o; o += put_box(t_tables + o, P.npy, ys); align();
-    o_kx = o; o += put_interp(t_tables + o, P.n2x, P.nx2); align();
-    o_ky = o; o += put_interp(t_tables + o, P.n2y, P.ny2); align();
-    const size_t table_bytes = o * sizeof(float2);
+    // tables at the start of the array, computed on the device
+    const TableSet ts = table_set(P.npx, P.npy, P.ri, xs, ys, P.n2x, P.nx2, P.n2y, P.ny2);
+    const size_t table_bytes = (size_t)ts.total * sizeof(float2);
 
     // per-window scratch, same arrays as a context batch
     const size_t nw = (size_t)nlocs;
@@ -187,7 +257,7 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
     const size_t s_md = take(64 * sizeof(float));
     const size_t s_mdnext = take(64);
     const size_t s_corr0n = take(sizeof(double));
-    if (o > kMaxTable || off > (size_t)XCG_NOALLOC_SCRATCH_BYTES) {
+    if (off > (size_t)XCG_NOALLOC_SCRATCH_BYTES) {
         const size_t per = (off - a256(table_bytes)) / nw;
         snprintf(t_msg, sizeof t_msg,
                  "%d windows need %zu bytes of scratch; the fixed array holds %zu bytes (at most %zu windows of this size per call)",
@@ -197,11 +267,10 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
     }
 
     cudaStream_t s = (cudaStream_t)stream;
-    cudaError_t e = cudaMemcpyAsync(base, t_tables, table_bytes, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) { snprintf(t_msg, sizeof t_msg, "table upload: %s", cudaGetErrorString(e)); return fail_msg(XCG_ERR_CUDA); }
-    const float2 *tb = (const float2 *)base;
-    P.tw_row = tb + o_twr; P.tw_col = tb + o_twc; P.phase = tb + o_ph;
-    P.box_x = tb + o_bx; P.box_y = tb + o_by; P.kx = tb + o_kx; P.ky = tb + o_ky;
+    float2 *tb = (float2 *)base;
+    k_noalloc_tables<<<(ts.total + 255) / 256, 256, 0, s>>>(ts, tb);
+    P.tw_row = tb + ts.off[T_TWR]; P.tw_col = tb + ts.off[T_TWC]; P.phase = tb + ts.off[T_PH];
+    P.box_x = tb + ts.off[T_BX]; P.box_y = tb + ts.off[T_BY]; P.kx = tb + ts.off[T_KX]; P.ky = tb + ts.off[T_KY];
     P.zrow = (float2 *)(base + s_zrow);
     P.amp1 = (float *)(base + s_amp1);
     P.amp2c = (float *)(base + s_amp2c);
@@ -225,7 +294,7 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
     P.winref = nullptr;
     P.locs = d_locs; P.nwin = nlocs; P.win0 = 0;
 
-    e = xcg::kernels_setup(P);
+    cudaError_t e = xcg::kernels_setup(P);
     if (e != cudaSuccess) { snprintf(t_msg, sizeof t_msg, "kernel attributes: %s", cudaGetErrorString(e)); return fail_msg(XCG_ERR_CUDA); }
     xcg::launch_rows(P, s);
     xcg::launch_cols(P, s);

@@ -27,9 +27,10 @@ EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_cre
            "xcg_stack_autotune", "xcg_stack_get_stats", "xcg_set_features", "xcg_refiner_create",
            "xcg_refiner_destroy", "xcg_refiner_set_params", "xcg_refiner_get_params", "xcg_refiner_forward",
            "xcg_refiner_gradient", "xcg_refiner_train_step", "xcg_correlate_device_refined",
-           "xcg_fit_offsets", "xcg_tc_gemm_check", "xcg_set_dft_form")
+           "xcg_fit_offsets", "xcg_tc_gemm_check", "xcg_set_dft_form", "xcg_debug_inject_stage_timeout")
 REFINER_NPARAM = 37507
 FLAG_REFINED = 4
+FLAG_STAGE_TIMEOUT = 8
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
@@ -159,6 +160,7 @@ def load(path: str | None = None):
                                   ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
     L.xcg_tc_gemm_check.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 4
     L.xcg_set_dft_form.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    L.xcg_debug_inject_stage_timeout.argtypes = [ctypes.c_void_p]
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
     _lib = L
@@ -212,6 +214,10 @@ class Context:
     def set_dft_form(self, form: int):
         """0: FP32 SIMT FFTs (default); 1: split-FP16 tensor-core DFTs (precision form)."""
         _check(self._L.xcg_set_dft_form(self._h, int(form)))
+
+    def inject_stage_timeout(self):
+        """The next precision-form call behaves as if a tensor-core wait had run out (error-path tests)."""
+        self._L.xcg_debug_inject_stage_timeout(self._h)
 
     def stats(self) -> Stats:
         s = Stats()

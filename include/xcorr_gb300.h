@@ -55,7 +55,9 @@ typedef struct {
 
 enum { XCG_FLAG_OOB = 1,        /* part of a patch fell outside its image and was zero-filled */
        XCG_FLAG_NEXTREAD = 2,   /* the 8x8 neighbourhood used the next window's first surface value */
-       XCG_FLAG_REFINED = 4 };  /* xfrac/yfrac come from the subpixel refiner, not the FFT interpolation */
+       XCG_FLAG_REFINED = 4,    /* xfrac/yfrac come from the subpixel refiner, not the FFT interpolation */
+       XCG_FLAG_STAGE_TIMEOUT = 8 };  /* precision form: a tensor-core stage's bounded wait ran out during this
+                                         call, so this window's surface may be incomplete; the result is not valid */
 
 /* Per-location result. */
 typedef struct {
@@ -145,9 +147,11 @@ xcg_status xcg_correlate_device(xcg_ctx *ctx,
  * per call.  A call needing more returns XCG_ERR_TOO_LARGE and
  * xcg_last_error() says how many windows fit.  The first call on each device
  * looks the array up (set-up work, so make it before any stream capture).
- * Calls share the array: two calls that overlap on the GPU race and must be
- * serialised by the caller.  Enqueued on `stream` (a cudaStream_t) of the
- * current device; returns after enqueueing. */
+ * Every call computes its transform tables on the device into the array (no
+ * copy from host memory), then runs the correlation kernels; the host does
+ * not wait for the stream.  Calls share the array: two calls that overlap on
+ * the GPU race and must be serialised by the caller.  Enqueued on `stream` (a
+ * cudaStream_t) of the current device; returns after enqueueing. */
 xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
                                         const void *d_master, int32_t m_nx, int32_t m_ny,
                                         const void *d_slave, int32_t s_nx, int32_t s_ny,
@@ -275,6 +279,14 @@ xcg_status xcg_fit_offsets(const xcg_result *d_results, const xcg_loc *d_locs, i
  * square windows of 64 or 128 (xsearch = ysearch = 32 or 64: 128- or
  * 256-point transforms); other shapes return XCG_ERR_UNSUPPORTED. */
 xcg_status xcg_set_dft_form(xcg_ctx *ctx, int32_t form);
+
+/* Diagnostic: the next call on this context that uses the precision form
+ * proceeds as if one of its tensor-core waits had run out (the error flag the
+ * stages raise is set on the host side instead of cleared at the start of the
+ * call): its windows carry XCG_FLAG_STAGE_TIMEOUT and xcg_correlate returns
+ * XCG_ERR_CUDA.  The call after it clears the flag again.  For tests of the
+ * error path; nothing on the device times out. */
+void xcg_debug_inject_stage_timeout(xcg_ctx *ctx);
 
 /* Diagnostic: the split-FP16 tensor-core GEMM engine of the precision form
  * (tcgen05, FP32 accumulation in tensor memory) on caller matrices:

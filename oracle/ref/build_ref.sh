@@ -12,9 +12,9 @@
 #   * -fcommon, because gmtsar_d.h:60-71 defines globals in a header.
 # The hook renames are -D flags on the calling translation units only.
 #
-# usage: oracle/ref/build_ref.sh [REFERENCE_SOURCE_DIR] [--host-only]
+# usage: oracle/ref/build_ref.sh REFERENCE_SOURCE_DIR [--host-only]
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:?usage: build_ref.sh REFERENCE_SOURCE_DIR [--host-only]}
 MODE=${2:-all}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$(cd "$HERE/.." && pwd)/_ref

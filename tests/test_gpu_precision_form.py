@@ -2,9 +2,8 @@
 column transforms) on the 128x128-window golden case, against the
 reference's own outputs, the FP32 SIMT path and the FP64 oracle.  Split FP16
 carries about 22 bits per operand, so the surface differs from the FP32
-path's at the 1e-6 level: integer peaks must match the reference except
-where the FP64 oracle itself calls a near-tie, and the subpixel offsets must
-stay within the reference's 0.01 px of the FP32 path."""
+path's at the 1e-6 level; on this case that changes no peak: integer peaks
+equal the reference's and subpixel peaks the FP32 path's, all 1000 of them."""
 import numpy as np
 import pytest
 
@@ -38,9 +37,9 @@ def test_precision_form_matches_reference(cfg1):
     g, m, s, locs, d, r32, rtc, _ = cfg1
     ip, jp = g["col"]("ip").astype(np.int32), g["col"]("jp").astype(np.int32)
     bad = np.where((rtc["ip"] != ip) | (rtc["jp"] != jp))[0]
-    assert len(bad) <= 2, bad
-    same = (rtc["fip"] == r32["fip"]) & (rtc["fjp"] == r32["fjp"])
-    assert same.mean() >= 0.99, same.mean()
+    assert len(bad) == 0, bad
+    np.testing.assert_array_equal(rtc["fip"], r32["fip"])
+    np.testing.assert_array_equal(rtc["fjp"], r32["fjp"])
     xo_t, yo_t = xg.output_offsets(rtc, 2, 0, 0, locs[:, 1], 0.0)
     xo_f, yo_f = xg.output_offsets(r32, 2, 0, 0, locs[:, 1], 0.0)
     assert np.max(np.abs(xo_t - xo_f)) <= 0.0625 and np.mean(np.abs(xo_t - xo_f) <= 0.01) >= 0.99
@@ -124,3 +123,33 @@ def test_precision_form_rejects_other_shapes():
     with xg.Context(xg.params(32, 64)) as ctx:
         with pytest.raises(xg.XcgError):
             ctx.set_dft_form(1)
+
+
+def test_stage_timeout_is_reported_then_cleared(cfg1):
+    """A tensor-core wait that runs out (injected on the host: the flag the
+    stages raise is set at the start of the call) fails the host entry, marks
+    every window of the device entry, and does not outlive its call."""
+    torch = pytest.importorskip("torch")
+    g, m, s, locs, d, r32, rtc, _ = cfg1
+    sub = locs[:40]
+    with xg.Context(xg.params(64, 64)) as ctx:
+        ctx.set_dft_form(1)
+        ctx.inject_stage_timeout()
+        with pytest.raises(xg.XcgError, match="wait ran out"):
+            ctx.correlate(m, s, sub, strip_len=d["nxl"])
+        r = ctx.correlate(m, s, sub, strip_len=d["nxl"])          # the next call is clean
+        assert not (r["flags"] & xg.FLAG_STAGE_TIMEOUT).any()
+        np.testing.assert_array_equal(r["ip"], rtc["ip"][:40])
+        dev = torch.device("cuda", 0)
+        dm, ds = torch.from_numpy(m).to(dev), torch.from_numpy(s).to(dev)
+        dl = torch.from_numpy(np.ascontiguousarray(sub)).to(dev)
+        out = torch.zeros((len(sub), xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+        sp = torch.cuda.current_stream(dev).cuda_stream
+        for inject in (True, False):
+            if inject:
+                ctx.inject_stage_timeout()
+            ctx.correlate_device(dm.data_ptr(), m.shape[1], m.shape[0], ds.data_ptr(), s.shape[1], s.shape[0],
+                                 dl.data_ptr(), len(sub), out.data_ptr(), sp, strip_len=d["nxl"])
+            torch.cuda.synchronize()
+            fl = np.frombuffer(out.cpu().numpy().tobytes(), dtype=xg.RESULT_DTYPE)["flags"]
+            assert ((fl & xg.FLAG_STAGE_TIMEOUT) != 0).all() == inject and ((fl & xg.FLAG_STAGE_TIMEOUT) != 0).any() == inject

@@ -8,6 +8,8 @@ the library.  Here it must give the same results as the context entry point
 first call's leftovers in the shared array -- and refuse a call that does not
 fit with a clear error.  The test allocates inputs and outputs itself (torch),
 as such a caller would.  This file is named to be collected last."""
+import time
+
 import numpy as np
 import pytest
 
@@ -71,3 +73,37 @@ def test_noalloc_refuses_more_than_its_fixed_scratch():
     with pytest.raises(xg.XcgError, match="size exceeds a fixed limit.*at most"):
         xg.correlate_device_noalloc(p, img.data_ptr(), 2048, 4096, img.data_ptr(), 2048, 4096,
                                     locs.data_ptr(), 64, out.data_ptr(), 0)
+
+
+def test_noalloc_call_does_not_wait_for_the_stream():
+    """The entry copies nothing from host memory (its tables are computed on
+    the device), so a call queued behind long-running work returns at once and
+    still gives the context entry's results once the stream drains."""
+    torch = pytest.importorskip("torch")
+    g = gu.load("xs32")
+    m, s, locs, d, xoff, yoff, ast = gu.case_inputs("xs32", g)
+    p = xg.params(d["xsearch"], d["ysearch"], d["ri"], d["interp_flag"], d["ifc"])
+    dev = torch.device("cuda", 0)
+    dm, ds = torch.from_numpy(m).to(dev), torch.from_numpy(s).to(dev)
+    dl = torch.from_numpy(locs).to(dev)
+    n = len(locs)
+    stream = torch.cuda.Stream(dev)
+    sp = stream.cuda_stream
+    got = torch.zeros((n, xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+    args = (p, dm.data_ptr(), m.shape[1], m.shape[0], ds.data_ptr(), s.shape[1], s.shape[0], dl.data_ptr(), n,
+            got.data_ptr(), sp, xoff, yoff, ast)
+    xg.correlate_device_noalloc(*args, strip_len=d["nxl"])       # set-up call
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        got.fill_(0xA5)                          # so the results read below are the second call's
+        torch.cuda._sleep(400_000_000)           # about 0.2 s of queued GPU work at 2 GHz
+    t0 = time.perf_counter()
+    xg.correlate_device_noalloc(*args, strip_len=d["nxl"])
+    host_s = time.perf_counter() - t0
+    stream.synchronize()
+    total_s = time.perf_counter() - t0
+    assert total_s > 0.05, "the queued work did not run"
+    assert host_s < 0.5 * total_s, f"the call waited for the stream: {host_s:.3f} s of {total_s:.3f} s"
+    r = _to_host(got)
+    np.testing.assert_array_equal(r["ip"], g["col"]("ip").astype(np.int32))
+    np.testing.assert_array_equal(r["fjp"], g["col"]("fjp").astype(np.int32))
