@@ -69,27 +69,94 @@ def _env_rank():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
-    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
-             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    """SM clocks and clock-event (throttle) reasons sampled DURING a timed
+    region: a thread reads them every millisecond in-process through NVML's
+    read-only queries (nvmlDeviceGetClockInfo, nvmlDeviceGetMaxClockInfo,
+    nvmlDeviceGetCurrentClocksEventReasons); where NVML cannot be loaded,
+    nvidia-smi is polled every 50 ms instead."""
+    SMI_FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    REASON_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+                   "hw_thermal_slowdown": 0x40, "hw_power_brake_slowdown": 0x80}
 
-    def __init__(self, gpu_index):
-        self.gpu = gpu_index
+    def __init__(self, cuda_index):
+        self.cuda_index = cuda_index
+        self.nvml = None
+        self.handle = None
         self.proc = None
-        self.path = os.path.join("/tmp", f"xcg_clocks_{os.getpid()}.csv")
+        self.samples = []
+        self._stop = None
+        try:
+            import ctypes
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                raise OSError("nvmlInit failed")
+            h = ctypes.c_void_p()
+            rc = 1
+            try:                       # the NVML device of this CUDA device, by UUID
+                import torch
+                uuid = str(torch.cuda.get_device_properties(cuda_index).uuid)
+                rc = lib.nvmlDeviceGetHandleByUUID(("GPU-" + uuid).encode(), ctypes.byref(h))
+            except Exception:
+                rc = 1
+            if rc != 0:
+                rc = lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(cuda_index), ctypes.byref(h))
+            if rc != 0:
+                raise OSError("no NVML handle")
+            self.nvml, self.handle = lib, h
+            self._reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        except Exception:
+            self.nvml = None
+
+    def _read(self):
+        import ctypes
+        mhz, reasons = ctypes.c_uint(), ctypes.c_ulonglong()
+        if self.nvml.nvmlDeviceGetClockInfo(self.handle, 1, ctypes.byref(mhz)) != 0:
+            return None
+        if self._reasons(self.handle, ctypes.byref(reasons)) != 0:
+            reasons.value = 0
+        return (float(mhz.value), int(reasons.value))
 
     def start(self):
+        self.samples = []
+        if self.nvml is not None:
+            import threading
+            self._stop = threading.Event()
+
+            def loop():
+                while not self._stop.is_set():
+                    v = self._read()
+                    if v:
+                        self.samples.append(v)
+                    self._stop.wait(0.001)
+            self._thread = threading.Thread(target=loop, daemon=True)
+            self._thread.start()
+            return
+        self.path = os.path.join("/tmp", f"xcg_clocks_{os.getpid()}.csv")
         try:
             self.f = open(self.path, "w")
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.cuda_index), f"--query-gpu={self.SMI_FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
     def stop(self):
+        if self.nvml is not None:
+            self._stop.set()
+            self._thread.join(timeout=5)
+            import ctypes
+            mx = ctypes.c_uint()
+            smax = float(mx.value) if self.nvml.nvmlDeviceGetMaxClockInfo(self.handle, 1, ctypes.byref(mx)) == 0 else None
+            sm = [v for v, _ in self.samples]
+            reasons = sorted({n for _, r in self.samples for n, b in self.REASON_BITS.items() if r & b})
+            return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": reasons,
+                    "samples": len(sm), "sm_mhz_min": min(sm) if sm else None,
+                    "source": "in-process NVML reads every 1 ms during the timed region"}
         if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock reader unavailable"], "samples": 0}
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -111,10 +178,10 @@ class ClockSampler:
                 if x.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi every 50 ms"}
 
 
-def cpu_baseline(m, s, locs, target_s=8.0):
+def cpu_baseline(m, s, locs, target_s=12.0):
     """The oracle's FP32 restatement on every host core, repeated over the
     workload's windows until about target_s seconds have passed."""
     import xcorr_oracle as xo
@@ -150,27 +217,34 @@ def read_traffic():
     return None
 
 
-def _timed(step, flush, stream, steps, warmup):
-    """Device time (ms) of `steps` calls of step(), L2 flushed before each."""
+def _timed(step, flush, stream, steps, warmup, clocks=None):
+    """Device time (ms) of `steps` calls of step(), L2 flushed before each;
+    clocks (a ClockSampler) is sampled over the timed steps."""
     import torch
     for _ in range(warmup):
         flush.zero_()
         step()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    if clocks:
+        clocks.start()
     for i in range(steps):
         flush.zero_()
         ev[i][0].record(stream)
         step()
         ev[i][1].record(stream)
     torch.cuda.synchronize()
+    if clocks:
+        clocks.clk = clocks.stop()
     return sum(a.elapsed_time(b) for a, b in ev)
 
 
-def run_frame(args):
+def frame_measure(steps, warmup, max_batch=0, e2e_calls=3):
     """Full-frame workload: 10240 x 30720 complex-int16 pair with the shift
     field dx = 2.1 + 1e-5 x - 3e-6 y, dy = -4.7 + 2e-6 x + 8e-6 y at 20 dB
-    SNR, 100 x 400 = 40,000 windows of 256 x 256 (512 x 512 transforms)."""
+    SNR, 100 x 400 = 40,000 windows of 256 x 256 (512 x 512 transforms).
+    Returns its JSON line (device-timed value, end-to-end value through the
+    host-buffer entry, per-kernel times, clocks)."""
     import torch
     import xcorr_gb300 as xg
     from xcorr_gb300 import synth
@@ -180,7 +254,7 @@ def run_frame(args):
     gen_s = time.perf_counter() - t0
     locs = xg.grid(10240, 30720, 100, 400, 128, 128)
     nwin = len(locs)
-    ctx = xg.Context(xg.params(128, 128), device=dev.index, max_batch=args.max_batch)
+    ctx = xg.Context(xg.params(128, 128), device=dev.index, max_batch=max_batch)
     dm, ds = torch.from_numpy(m).to(dev), torch.from_numpy(s).to(dev)
     dl = torch.from_numpy(locs).to(dev)
     dr = torch.zeros((nwin, xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
@@ -191,27 +265,28 @@ def run_frame(args):
         ctx.correlate_device(dm.data_ptr(), 10240, 30720, ds.data_ptr(), 10240, 30720, dl.data_ptr(), nwin,
                              dr.data_ptr(), stream.cuda_stream, strip_len=100)
     clocks = ClockSampler(dev.index)
-    clocks.start()
-    ms = _timed(step, flush, stream, args.steps, args.warmup)
-    clk = clocks.stop()
+    ms = _timed(step, flush, stream, steps, warmup, clocks)
+    clk = clocks.clk
     ctx.set_profiling(True)
     flush.zero_()
     step()
     st = ctx.stats()
     ctx.set_profiling(False)
     # end to end through the host entry point (2.5 GB of images in per call)
+    del dm, ds
     pm, ps = torch.from_numpy(m).pin_memory(), torch.from_numpy(s).pin_memory()
     pmn, psn = pm.numpy(), ps.numpy()
     ctx.correlate(pmn, psn, locs, strip_len=100)
     e2e_runs = []
-    for _ in range(3):                           # median of three calls
+    for _ in range(e2e_calls):                   # median of the calls
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         ctx.correlate(pmn, psn, locs, strip_len=100)
         e2e_runs.append(time.perf_counter() - t1)
-    e2e_s = sorted(e2e_runs)[1]
-    line = {"metric": "xcorr windows/s, full frame, 256^2 windows (512^2 FFT)", "value": args.steps * nwin / (ms / 1e3),
-            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+    e2e_s = sorted(e2e_runs)[len(e2e_runs) // 2]
+    ctx.close()
+    return {"metric": "xcorr windows/s, full frame, 256^2 windows (512^2 FFT)", "value": steps * nwin / (ms / 1e3),
+            "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "full frame", "image": "10240x30720 complex int16, varying shift, 20 dB",
                        "windows": nwin, "xsearch": 128, "ysearch": 128, "range_interp": 2, "interp": 16,
@@ -219,9 +294,56 @@ def run_frame(args):
             "kernel_ms_per_step": {n: st.kernel_ms[i] for i, n in enumerate(xg.KERNEL_NAMES)},
             "batches_per_step": st.batches,
             "e2e": {"value": nwin / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(m.nbytes + s.nbytes + locs.nbytes),
-                    "d2h_bytes_per_step": int(nwin * xg.RESULT_DTYPE.itemsize), "timer": "host wall clock, median of 3 calls"},
+                    "d2h_bytes_per_step": int(nwin * xg.RESULT_DTYPE.itemsize),
+                    "timer": f"host wall clock, median of {e2e_calls} calls"},
             "clocks": clk}
-    print(json.dumps(line), flush=True)
+
+
+def run_frame(args):
+    print(json.dumps(frame_measure(args.steps, args.warmup, args.max_batch)), flush=True)
+
+
+def program_times(runs=3):
+    """Whole-program wall time of the drop-in xcorr program on the headline
+    case (its SLC and PRM files written to a scratch directory, read from the
+    page cache), and of the reference's own GPU program (oracle/_ref/xcorr-gpu)
+    on the same files when it has been built on this machine (build() builds
+    it where XCG_REFERENCE_SOURCES names the reference sources)."""
+    import shutil
+    import tempfile
+    from xcorr_gb300 import synth
+    prog = {"ours": os.path.join(ROOT, "gmtsar-gpu_gb300", "bin", "xcorr"),
+            "reference": os.path.join(ROOT, "oracle", "_ref", "xcorr-gpu")}
+    out = {"case": "2048x4096 pair, -nx 20 -ny 50 (1000 windows of 128x128), files in the page cache",
+           "timer": f"wall clock of the whole program, median of {runs} runs"}
+    d = tempfile.mkdtemp(prefix="xcg_bench_")
+    try:
+        synth.write_case(d, synth.PairSpec(**SPEC))
+        for name, exe in prog.items():
+            if not os.access(exe, os.X_OK):
+                out[name] = {"unavailable": ("the reference program is built only where its sources are "
+                                             "present (XCG_REFERENCE_SOURCES at build time); not on this machine")
+                             if name == "reference" else "bin/xcorr not built"}
+                continue
+            ts = []
+            for _ in range(runs + 1):               # the first run warms the page cache and the driver
+                t0 = time.perf_counter()
+                r = subprocess.run([exe, "master.PRM", "aligned.PRM", "-nx", "20", "-ny", "50"], cwd=d,
+                                   capture_output=True, text=True, timeout=120)
+                ts.append(time.perf_counter() - t0)
+                if r.returncode != 0:
+                    break
+            if r.returncode != 0:
+                out[name] = {"unavailable": f"exit status {r.returncode}: {r.stderr.strip()[-200:]}"}
+                continue
+            lines = open(os.path.join(d, "freq_xcorr.dat")).read().splitlines()
+            out[name] = {"wall_s": sorted(ts[1:])[runs // 2], "windows": len(lines),
+                         "windows_per_s": len(lines) / sorted(ts[1:])[runs // 2]}
+    except Exception as e:  # noqa: BLE001 - reported, not fatal
+        out["error"] = str(e)[:200]
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return out
 
 
 def run_stack(args):
@@ -271,9 +393,8 @@ def run_stack(args):
         stack.set_graph(True)
         flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
         clocks = ClockSampler(dev.index)
-        clocks.start()
-        ms = _timed(lambda: stack.run(pairs, stream.cuda_stream), flush, stream, args.steps, args.warmup)
-        clk = clocks.stop()
+        ms = _timed(lambda: stack.run(pairs, stream.cuda_stream), flush, stream, args.steps, args.warmup, clocks)
+        clk = clocks.clk
     st = stack.stats()
     img_gb = sum(it[0].numel() * 2 * 2 for it in items) / 1e9
     line = {"metric": "xcorr windows/s, stack of 32 pairs, mixed 64/128/256 windows", "value": args.steps * total / (ms / 1e3),
@@ -290,6 +411,10 @@ def run_stack(args):
 
 
 def run_reference(args):
+    """The reference path on the host cores: the oracle's FP32 restatement of
+    the reference's algorithm (the reference has no CPU implementation of the
+    frequency-domain path), OpenMP over windows on every core, each step the
+    whole 1000-window workload."""
     rank, world, _ = _env_rank()
     if rank != 0:
         return
@@ -300,25 +425,23 @@ def run_reference(args):
     locs = xg.grid(2048, 4096, 20, 50)
     p = xo.params(64, 64, 2, 1, 16)
     cores = os.cpu_count() or 1
-    sample = 64
-    idx = np.linspace(0, len(locs) - 1, sample).astype(int)
-    sl = locs[idx]
     for _ in range(args.warmup):
-        xo.run(p, m, s, sl, precision=xo.F32, nthreads=cores)
+        xo.run(p, m, s, locs, precision=xo.F32, nthreads=cores, strip_len=20)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        xo.run(p, m, s, sl, precision=xo.F32, nthreads=cores)
+        xo.run(p, m, s, locs, precision=xo.F32, nthreads=cores, strip_len=20)
         times.append(time.perf_counter() - t0)
     tot = sum(times)
-    value = args.steps * sample / tot
+    value = args.steps * len(locs) / tot
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
-            "config": dict(WORKLOAD, step_sample=f"{sample} of the 1000 windows per step"),
+            "config": dict(WORKLOAD, l2="not applicable (host cores)"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{sample} windows per step, oracle FP32 restatement of the reference path "
-                                       "(the reference has no CPU implementation of this path), OpenMP"},
+                             "sample": f"the whole {len(locs)}-window workload every step, oracle FP32 restatement "
+                                       "of the reference path (the reference has no CPU implementation of this "
+                                       "path), OpenMP over windows"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
     print(json.dumps(line), flush=True)
@@ -353,11 +476,11 @@ def run_ours(args):
                              dr.data_ptr(), sp, strip_len=20)
 
     clocks = ClockSampler(dev.index)
-    clocks.start()                 # sampled through warm-up and the timed steps
     for _ in range(args.warmup):
         flush.zero_()
         step()
     torch.cuda.synchronize()
+    clocks.start()                 # sampled over the timed steps
 
     # device-timed steps
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -395,6 +518,11 @@ def run_ours(args):
             kms[k] += st.kernel_ms[k]
     ctx.set_profiling(False)
     nprof = max(3, min(args.steps, 20))
+    # the FP32 SIMT ceiling of the roofline, measured on this GPU by the library's FMA kernel
+    try:
+        fma_tflops = xg.fp32_fma_rate(dev.index)
+    except xg.XcgError:
+        fma_tflops = None
 
     # the surrogate form: the trained subpixel refiner in place of the FFT
     # interpolation where it is confident (same workload, same timing rules)
@@ -516,14 +644,19 @@ def run_ours(args):
         avg_ms = kms[dom] / nprof / batches
         ach = fl[dom_name] * wpl / (avg_ms / 1e3) / 1e12
         smax = peaks.get("sm_max_mhz", 2070.0)
-        fp32_peak = 152 * 128 * 2 * smax * 1e6 / 1e12
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        nominal = sms * 128 * 2 * smax * 1e6 / 1e12
+        fp32_peak = fma_tflops if fma_tflops else nominal
         tpw = read_traffic()
         traffic = tpw * wpl if tpw else None
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"bound": "fp32_simt", "kernel": dom_name, "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": ach / fp32_peak, "traffic": traffic,
-                "peak_source": "nominal FP32 SIMT rate, 152 SMs x 128 lanes x 2 flop at the measured max SM clock "
-                               f"({smax:.0f} MHz, MEASURED_PEAKS.json); MEASURED_PEAKS.json has no FP32 figure",
+                "peak_source": (f"of measured: FP32 FMA rate of this GPU from the library's own FMA kernel "
+                                f"(xcg_fp32_fma_rate, CUDA events); nominal {nominal:.1f} TFLOP/s = {sms} SMs x 128 "
+                                f"lanes x 2 flop x {smax:.0f} MHz") if fma_tflops else
+                               f"nominal FP32 SIMT rate, {sms} SMs x 128 lanes x 2 flop x {smax:.0f} MHz",
+                "fp32_nominal": nominal, "frac_of_nominal": ach / nominal,
                 "algorithmic": f"{fl[dom_name] / 1e6:.2f} MFLOP/window x {wpl:.0f} windows per launch "
                                f"({batches} launches per {nwin}-window step)",
                 "avg_launch_ms": avg_ms,
@@ -540,6 +673,13 @@ def run_ours(args):
                 "roofline": roof, "clocks": clk, "gpu_launches": launches, "surrogate": surrogate,
                 "precision_form": precision,
                 "wall_s_timed": wall}
+        if world == 1 and not args.no_frame:
+            fr = frame_measure(3, 3, e2e_calls=3)
+            line["frame"] = {k: fr[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup",
+                                                 "kernel_ms_per_step", "e2e", "clocks")}
+            line["frame"]["windows"] = fr["config"]["windows"]
+        if world == 1 and not args.no_programs:
+            line["programs"] = program_times()
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(m, s, locs)
         print(json.dumps(line), flush=True)
@@ -551,7 +691,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="headline", choices=["headline", "frame", "stack"],
@@ -560,6 +700,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the refined-path measurement")
     ap.add_argument("--no-precision-form", action="store_true", help="skip the tensor-core DFT measurement")
+    ap.add_argument("--no-frame", action="store_true", help="skip the full-frame measurement in the default line")
+    ap.add_argument("--no-programs", action="store_true", help="skip the whole-program timings in the default line")
     ap.add_argument("--max-batch", type=int, default=0,
                     help="windows per scratch slot (0: library default); small values keep profiler captures small")
     args = ap.parse_args()

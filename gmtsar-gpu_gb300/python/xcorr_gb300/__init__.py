@@ -27,7 +27,8 @@ EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_cre
            "xcg_stack_autotune", "xcg_stack_get_stats", "xcg_set_features", "xcg_refiner_create",
            "xcg_refiner_destroy", "xcg_refiner_set_params", "xcg_refiner_get_params", "xcg_refiner_forward",
            "xcg_refiner_gradient", "xcg_refiner_train_step", "xcg_correlate_device_refined",
-           "xcg_fit_offsets", "xcg_tc_gemm_check", "xcg_set_dft_form", "xcg_debug_inject_stage_timeout")
+           "xcg_fit_offsets", "xcg_tc_gemm_check", "xcg_set_dft_form", "xcg_debug_inject_stage_timeout",
+           "xcg_fp32_fma_rate")
 REFINER_NPARAM = 37507
 FLAG_REFINED = 4
 FLAG_STAGE_TIMEOUT = 8
@@ -161,6 +162,8 @@ def load(path: str | None = None):
     L.xcg_tc_gemm_check.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 4
     L.xcg_set_dft_form.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_debug_inject_stage_timeout.argtypes = [ctypes.c_void_p]
+    L.xcg_fp32_fma_rate.restype = ctypes.c_int
+    L.xcg_fp32_fma_rate.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
     _lib = L
@@ -380,6 +383,13 @@ def fit_offsets(d_results: int, d_locs: int, nlocs: int, d_out: int, ri=2, x_off
 def tc_gemm_check(m_tiles: int, n_tile: int, k: int, n_total: int, d_a: int, d_b: int, d_c: int, stream: int = 0):
     """xcg_tc_gemm_check: the split-FP16 tcgen05 GEMM engine on FP32 device matrices."""
     _check(load().xcg_tc_gemm_check(m_tiles, n_tile, k, n_total, d_a, d_b, d_c, stream))
+
+
+def fp32_fma_rate(device: int = 0) -> float:
+    """xcg_fp32_fma_rate: measured FP32 FMA throughput of the device, TFLOP/s."""
+    v = ctypes.c_double()
+    _check(load().xcg_fp32_fma_rate(device, ctypes.byref(v)))
+    return v.value
 
 
 def grid(m_nx, m_ny, nxl, nyl, xsearch=64, ysearch=64):

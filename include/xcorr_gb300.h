@@ -296,6 +296,13 @@ void xcg_debug_inject_stage_timeout(xcg_ctx *ctx);
 xcg_status xcg_tc_gemm_check(int32_t m_tiles, int32_t n_tile, int32_t k, int32_t n_total,
                              const float *d_a, const float *d_b, float *d_c, void *stream);
 
+/* Diagnostic: FP32 fused multiply-add throughput of `device` (TFLOP/s, two
+ * flops per FMA), measured by a kernel of this library over tens of
+ * milliseconds (CUDA events, best of five launches after a warm-up): the
+ * FP32 SIMT ceiling against which the FFT kernels' rates are reported.  No
+ * counterpart in the reference. */
+xcg_status xcg_fp32_fma_rate(int32_t device, double *tflops);
+
 /* Record CUDA events around every kernel launch (adds a synchronisation at
  * the end of each correlate call to read them). */
 void xcg_set_profiling(xcg_ctx *ctx, int32_t enable);

@@ -17,7 +17,7 @@ HEADER = os.path.join(ROOT, "include", "xcorr_gb300.h")
 def declared_functions():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(xcg_[a-z_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(xcg_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_library_exports_every_declared_symbol():
