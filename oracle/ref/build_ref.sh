@@ -5,7 +5,9 @@
 #   oracle/_ref/xcorr-gpu-dump  the same objects plus oracle/ref/dump_hooks.cu,
 #                               which records per-location results at full precision
 # and oracle/_ref/ref_host_probe, the reference's host C functions (PRM parse,
-# location grid, result writer) behind a small driver for CPU parity tests.
+# location grid, result writer) behind a small driver for CPU parity tests, and
+# oracle/_ref/ref_time_probe, the reference's do_time_corr (-time / -time4) on
+# supplied integer patches.
 #
 # Two additions are needed for a current toolchain (both outside the sources):
 #   * oracle/ref/helper_cuda.h stands in for the CUDA-samples header named in gpu_err.h:9;
@@ -51,10 +53,15 @@ $NV -Dh_reduceCr_strip=xcg_hook_h_reduceCr_strip -c "$REF/highres_corr.cu" -o "$
 $NV -c "$HERE/dump_hooks.cu" -o "$OBJ/dump_hooks.o" &
 wait
 
+# time-domain probe: the reference's do_time_corr on supplied integer patches
+$CC -O2 -std=c99 -fcommon -w -I"$REF" -c "$HERE/ref_time_probe.c" -o "$OBJ/ref_time_probe.o"
+$NVCC "$OBJ/ref_time_probe.o" "$OBJ/do_time_int_xcorr.o" "$OBJ/conv_ampl_demean.o" "$OBJ/utils.o" "$OBJ/plxyz.o" \
+      -lm -o "$OUT/ref_time_probe"
+
 LIBC="$OBJ/get_locations.o $OBJ/parse_xcorr_input.o $OBJ/utils.o $OBJ/read_xcorr_data.o $OBJ/sio_struct.o $OBJ/plxyz.o"
 $NVCC "$OBJ/xcorr.o" "$OBJ/fft_interpolate_routines.o" "$OBJ/conv_ampl_demean.o" "$OBJ/do_freq_xcorr.o" \
       "$OBJ/do_time_int_xcorr.o" "$OBJ/highres_corr.o" $LIBC "$OBJ/print_results.o" -lm -lcufft -o "$OUT/xcorr-gpu"
 $NVCC "$OBJ/xcorr_dump.o" "$OBJ/fft_interpolate_routines.o" "$OBJ/conv_ampl_demean.o" "$OBJ/do_freq_xcorr_dump.o" \
       "$OBJ/do_time_int_xcorr.o" "$OBJ/highres_corr_dump.o" "$OBJ/dump_hooks.o" $LIBC "$OBJ/print_results_renamed.o" \
       -lm -lcufft -o "$OUT/xcorr-gpu-dump"
-echo "build_ref: built $OUT/xcorr-gpu $OUT/xcorr-gpu-dump $OUT/ref_host_probe"
+echo "build_ref: built $OUT/xcorr-gpu $OUT/xcorr-gpu-dump $OUT/ref_host_probe $OUT/ref_time_probe"

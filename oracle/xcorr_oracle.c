@@ -367,6 +367,13 @@ void xo_prepare_patch(const xo_params *p, int precision, int slave, const float 
     }
 }
 
+void xo_time_surface(const xo_params *p, const int32_t *i1, const int32_t *i2, double *corr, xo_result *r)
+{
+    memset(r, 0, sizeof *r);
+    time_surface(p, i1, i2, corr);
+    time_peak(p, corr, r);
+}
+
 void xo_surface(const xo_params *p, int precision, const float *pm_c, const float *ps_c,
                 double *corr, double *mean1, double *mean2)
 {

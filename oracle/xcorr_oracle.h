@@ -83,6 +83,11 @@ void xo_prepare_patch(const xo_params *p, int precision, int slave, const float 
 /* Correlation surface (nyc x nxc doubles) for one pair of complex patches. */
 void xo_surface(const xo_params *p, int precision, const float *pm_c, const float *ps_c,
                 double *corr, double *mean1, double *mean2);
+/* Full-search time-domain surface (nyc x nxc doubles) of the -time / -time4
+ * modes (p->corr_mode 0 / 1) on one window's (int) demeaned patches i1, i2
+ * (npy x npx each), and the peak do_time_corr picks (xoff, yoff, corr, ip,
+ * jp, cmax in r). */
+void xo_time_surface(const xo_params *p, const int32_t *i1, const int32_t *i2, double *corr, xo_result *r);
 /* The reference's argmax (value, index) over n elements in 2048-element blocks
  * with its exact tie-breaking; returns the flat index. */
 int64_t xo_argmax_ref(const double *x, int64_t n, double *vmax);

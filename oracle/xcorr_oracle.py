@@ -66,6 +66,8 @@ def lib():
                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_void_p, ctypes.c_void_p]
+        L.xo_time_surface.argtypes = [ctypes.POINTER(XoParams), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]
         L.xo_argmax_ref.restype = ctypes.c_int64
         L.xo_argmax_ref.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_double)]
         _lib = L
@@ -114,6 +116,17 @@ def prepare_patch(p: XoParams, patch: np.ndarray, slave: bool, precision=F32):
     lib().xo_prepare_patch(ctypes.byref(p), precision, int(slave), patch.ctypes.data, amp.ctypes.data,
                            ctypes.byref(mean), ints.ctypes.data)
     return amp, mean.value, ints
+
+
+def time_surface(p: XoParams, i1: np.ndarray, i2: np.ndarray):
+    """-time / -time4 (p.corr_mode 0 / 1) full-search surface of one window's
+    (int) patches (npy, npx) and do_time_corr's peak as a result record."""
+    i1 = np.ascontiguousarray(i1, dtype=np.int32)
+    i2 = np.ascontiguousarray(i2, dtype=np.int32)
+    corr = np.zeros((p.nyc, p.nxc), np.float64)
+    r = np.zeros(1, dtype=RESULT_DTYPE)
+    lib().xo_time_surface(ctypes.byref(p), i1.ctypes.data, i2.ctypes.data, corr.ctypes.data, r.ctypes.data)
+    return corr, r[0]
 
 
 def surface(p: XoParams, pm: np.ndarray, ps: np.ndarray, precision=F32):

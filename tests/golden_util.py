@@ -59,3 +59,22 @@ def case_inputs(name, g=None):
     xoff, yoff = (0, 0) if d["noshift"] else (g["rshift"], g["ashift"])
     ast = (g["prf_slave"] - g["prf_master"]) / g["prf_master"]
     return m, s, locs, d, xoff, yoff, ast
+
+
+def cut_patches(m, s, x, y, npx, npy, x_offset=0, y_offset=0, astretcha=0.0):
+    """The master and slave patches of location (x, y) as complex64 (npy, npx)
+    arrays, zero outside the images (xcorr.cu:330-338 on the lines
+    read_xcorr_data.c:52-85 reads; the slave row origin adds y_offset and
+    (int)(y * astretcha))."""
+    def cut(img, x0, y0):
+        out = np.zeros((npy, npx), np.complex64)
+        ny, nx = img.shape[:2]
+        ya, yb, xa, xb = max(y0, 0), min(y0 + npy, ny), max(x0, 0), min(x0 + npx, nx)
+        if ya < yb and xa < xb:
+            blk = img[ya:yb, xa:xb]
+            z = blk.astype(np.float32) if blk.ndim == 2 else blk[..., 0].astype(np.float32) + 1j * blk[..., 1].astype(np.float32)
+            out[ya - y0:yb - y0, xa - x0:xb - x0] = z
+        return out
+    ishft = int(y * astretcha)
+    return (cut(m, x - npx // 2, y - npy // 2),
+            cut(s, x + x_offset - npx // 2, y + y_offset + ishft - npy // 2))

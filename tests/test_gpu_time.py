@@ -86,3 +86,36 @@ def test_time_modes_larger_windows(xs, ys, mode):
         r = ctx.correlate(m, s, locs, strip_len=2)
     o = xo.run(xo.params(xs, ys, corr_mode=mode), m, s, locs, precision=xo.F32, strip_len=2)
     _compare(r, o, min_same=1.0, mode=mode)
+
+
+def test_time_modes_against_reference_functions():
+    """The GPU's -time / -time4 results on the windows whose surfaces the
+    reference's own do_time_corr produced (tests/golden/ref_time.json.gz, made
+    by tests/golden/make_ref_time.py from the oracle's integer patches): the
+    peak and struct locs fields the reference set, the correlation within the
+    tolerances above (the GPU forms its integers from its own interpolation)."""
+    import gzip
+    import json
+    import os
+    with gzip.open(os.path.join(gu.GOLDEN_DIR, "ref_time.json.gz"), "rt") as f:
+        recs = json.load(f)["records"]
+    by_case = {}
+    for rec in recs:
+        by_case.setdefault((rec["case"], rec["mode"]), []).append(rec)
+    for (case, mode), rs in by_case.items():
+        g = gu.load(case)
+        m, s, locs, d, xoff, yoff, ast = gu.case_inputs(case, g)
+        wins = [r["window"] for r in rs]
+        sub = np.ascontiguousarray(locs[wins])
+        p = xg.params(d["xsearch"], d["ysearch"], d["ri"], d["interp_flag"], d["ifc"], corr_mode=mode)
+        with xg.Context(p) as ctx:
+            r = ctx.correlate(m, s, sub, xoff, yoff, ast, strip_len=0)
+        for k, rec in enumerate(rs):
+            assert (float(r["xoff"][k]), float(r["yoff"][k])) == (rec["xoff"], rec["yoff"]), (case, mode, rec["window"])
+            want, got = rec["corr"], float(r["corr"][k])
+            if mode == 0 or want == 0.0:
+                assert abs(got - want) <= 1e-4 * max(abs(want), 1e-30) or got == want, (case, mode, got, want)
+            else:
+                ratio = lambda c: 0.5 * ((c / 100.0) ** 2 + 1.0)
+                assert abs(ratio(got) - ratio(want)) < 2e-5, (case, mode, got, want)
+            assert abs(float(r["cmax"][k]) - rec["surface_max"]) <= 1e-4 * max(rec["surface_max"], 1e-30)

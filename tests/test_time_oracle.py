@@ -1,10 +1,18 @@
 """The -time / -time4 restatement in the oracle (do_time_corr,
-do_time_int_xcorr.cu:146-189).  The reference's GPU build runs these modes
-without data, so they have no golden vectors; they are pinned here to the
-frequency path, which is: the full-search surface at the frequency path's
+do_time_int_xcorr.cu:146-189).  The reference's GPU program runs these modes
+without data, so its own functions were driven directly
+(oracle/_ref/ref_time_probe, tests/golden/make_ref_time.py) on the integer
+patches of golden windows: the oracle must reproduce their float64 surfaces
+bit for bit and the peak and correlation they set.  Beyond that it is pinned
+to the frequency path: the full-search surface at the frequency path's
 integer peak is the same calc_time_corr formula the frequency path evaluates
 there, so where both modes pick the same lag their correlation is identical,
 and on a clean pair both pick the true shift."""
+import gzip
+import hashlib
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -12,6 +20,34 @@ import golden_util as gu
 import xcorr_oracle as xo
 from xcorr_gb300 import synth
 from xcorr_gb300.synth import PairSpec
+
+
+def load_time_records():
+    with gzip.open(os.path.join(gu.GOLDEN_DIR, "ref_time.json.gz"), "rt") as f:
+        return json.load(f)["records"]
+
+
+def window_ints(case, w):
+    """The integer patches of one golden window as the fixture generator made them."""
+    g = gu.load(case)
+    m, s, locs, d, xoff, yoff, ast = gu.case_inputs(case, g)
+    x, y = (int(v) for v in locs[w])
+    p = xo.params(d["xsearch"], d["ysearch"], d["ri"])
+    pm, ps = gu.cut_patches(m, s, x, y, p.npx, p.npy, xoff, yoff, ast)
+    return d, locs[w], xo.prepare_patch(p, pm, False, xo.F32)[2], xo.prepare_patch(p, ps, True, xo.F32)[2]
+
+
+@pytest.mark.parametrize("rec", load_time_records(), ids=lambda r: f"{r['case']}-w{r['window']}-mode{r['mode']}")
+def test_time_surface_matches_reference_functions(rec):
+    d, loc, i1, i2 = window_ints(rec["case"], rec["window"])
+    assert hashlib.sha256(i1.tobytes()).hexdigest() == rec["i1_sha256"]
+    assert hashlib.sha256(i2.tobytes()).hexdigest() == rec["i2_sha256"]
+    p = xo.params(d["xsearch"], d["ysearch"], d["ri"], corr_mode=rec["mode"])
+    corr, r = xo.time_surface(p, i1, i2)
+    np.testing.assert_array_equal(corr.ravel()[rec["sample_index"]], np.array(rec["sample_value"]))
+    assert hashlib.sha256(corr.tobytes()).hexdigest() == rec["surface_sha256"], "surface differs in some bit"
+    assert float(np.abs(corr).max()) == rec["surface_max"]
+    assert (float(r["xoff"]), float(r["yoff"]), float(r["corr"])) == (rec["xoff"], rec["yoff"], rec["corr"])
 
 
 @pytest.fixture(scope="module")
