@@ -154,8 +154,8 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
     if (!p || !out) return XCG_ERR_ARG;
     *out = nullptr;
     const int xs = p->xsearch, ys = p->ysearch;
-    if (!pow2(xs) || !pow2(ys) || xs < 32 || ys < 32 || xs > 256 || ys > 256) {
-        g_last_error = "xsearch/ysearch must be powers of two in 32..256";
+    if (!pow2(xs) || !pow2(ys) || xs < 16 || ys < 16 || xs > 256 || ys > 256) {
+        g_last_error = "xsearch/ysearch must be powers of two in 16..256";
         return XCG_ERR_ARG;
     }
     if (p->nx_corr != 2 * xs || p->ny_corr != 2 * ys) {
@@ -170,6 +170,10 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
     if (p->n2x != 8 || p->n2y != 8) { g_last_error = "n2x = n2y = 8 only"; return XCG_ERR_UNSUPPORTED; }
     if (p->format != 0 && p->format != 1) { g_last_error = "format must be 0 or 1"; return XCG_ERR_ARG; }
     if (p->corr_mode < 0 || p->corr_mode > 2) { g_last_error = "corr_mode must be 0 (-time), 1 (-time4) or 2"; return XCG_ERR_ARG; }
+    if (p->corr_mode < 2 && (xs < 32 || ys < 32)) {
+        g_last_error = "-time/-time4 need xsearch/ysearch of 32 or more (lag tiles of 32 x 64)";
+        return XCG_ERR_UNSUPPORTED;
+    }
 
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);

@@ -25,17 +25,14 @@
 #include "team_fft.cuh"
 #include "xcorr_kernels.cuh"
 
-#ifndef XCG_COLS_THREADS
-#define XCG_COLS_THREADS 128
-#endif
-#ifndef XCG_COLS_BLOCKS
+// Launch shapes a plan selects (Plan::cols_cfg, Plan::peak_cfg; the stack's
+// autotuner times them per window geometry):
+//   k_cols  0: 128 threads, staging in two cp.async groups (partner columns
+//              first), 5 CTAs/SM (the default); 1: 256 threads (twice the
+//              column pairs per CTA), two groups; 2: 128 threads, one group
+//   k_peak  0: 4 resident CTAs/SM (64 registers, a few spills; beats 3 for
+//              transforms up to 256 points); 1: 3 CTAs/SM (85 registers)
 #define XCG_COLS_BLOCKS 5
-#endif
-// k_peak: one CTA per window, so the grid is about one wave; 4 resident CTAs
-// per SM (64 registers, a few spills) beat 3 for transforms up to 256 points
-#ifndef XCG_PEAK_BLOCKS
-#define XCG_PEAK_BLOCKS 4
-#endif
 
 namespace xcg {
 
@@ -388,20 +385,23 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // shared memory with coalesced row reads, each FFT uses its own column slot as
 // the exchange buffer (the column is in registers meanwhile), and the half
 // spectrum goes back row by row.
-template <int M>
+template <int M, int THR = 128>
 struct ColsGeom {
     static constexpr int T = fft_lanes(M);
     static constexpr int PADM = fft_padded_len(M);
     static constexpr int CS = PADM + 1;
-    static constexpr int THREADS = XCG_COLS_THREADS;
+    static constexpr int THREADS = THR;
     static constexpr int CP = THREADS / T;        // column pairs per CTA = teams
     static constexpr int TWL = fft_twiddle_len(M);
-    static constexpr int BLOCKS = (M >= 1024) ? 2 * 128 / THREADS : (M >= 512 ? 3 * 128 / THREADS : XCG_COLS_BLOCKS);
+    static constexpr int BLOCKS = (M >= 1024) ? (THREADS >= 256 ? 1 : 2)
+                                : (M >= 512 ? (THREADS >= 256 ? 1 : 3) : XCG_COLS_BLOCKS * 128 / THREADS);
 };
 
-template <int M>
-__global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_cols(Plan P) {
-    using G = ColsGeom<M>;
+// DEPTH 2: partner and own columns staged as two cp.async groups, the partner
+// transforms overlapping the own columns' arrival; DEPTH 1: one group.
+template <int M, int THR, int DEPTH>
+__global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols(Plan P) {
+    using G = ColsGeom<M, THR>;
     constexpr int T = G::T, CS = G::CS, CP = G::CP, TWL = G::TWL;
     constexpr int PER = M / T;
     static_assert((CP & (CP - 1)) == 0 && T % 2 == 0, "column pairs per CTA: a power of two");
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
             const int r = row0 + k * RSTEP;
             cp_async8(cols + (CP + sl) * CS + fft_pad(r), base + (size_t)r * N + pcol);
         }
-        cp_async_commit();
+        if constexpr (DEPTH == 2) cp_async_commit();
 #pragma unroll 8
         for (int k = 0; k < NLD; k++) {
             const int r = row0 + k * RSTEP;
@@ -462,8 +462,9 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
             if (b == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
         }
     }
-    cp_async_wait<1>();                          // partner columns in (this thread's copies)
-    __syncthreads();                             // ... and everyone's
+    if constexpr (DEPTH == 2) cp_async_wait<1>();   // partner columns in (this thread's copies)
+    else cp_async_wait<0>();                        // all columns in
+    __syncthreads();                                // ... and everyone's
     const float dc1 = shf[0];
     const float m2 = shf[1];
 
@@ -478,8 +479,10 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
     team_fft_reg<M, -1>(z, pa, tw, lane);
 #pragma unroll
     for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
-    cp_async_wait<0>();                          // own columns in
-    __syncthreads();
+    if constexpr (DEPTH == 2) {
+        cp_async_wait<0>();                      // own columns in
+        __syncthreads();
+    }
 #pragma unroll
     for (int m = 0; m < PER; m++) z[m] = a[fft_pad(lane + T * m)];
     __syncwarp();
@@ -553,8 +556,8 @@ __global__ void __launch_bounds__(ColsGeom<M>::THREADS, ColsGeom<M>::BLOCKS) k_c
 // the per-window host loop of d_do_freq_corr_strip (do_freq_xcorr.cu:150-195),
 // the time correlation d_calc_time_corr_strip (do_time_int_xcorr.cu:71-100),
 // d_scaled_strip (conv_ampl_demean.cu:50-68) and d_cppow_strip (:75-95).
-template <int N>
-__global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 ? 2 : 1)) k_peak(Plan P) {
+template <int N, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
     constexpr int T = fft_lanes(N);
     constexpr int PADN = fft_padded_len(N);
     constexpr int TWL = fft_twiddle_len(N);
@@ -673,15 +676,17 @@ __global__ void __launch_bounds__(256, (N <= 256) ? XCG_PEAK_BLOCKS : (N <= 512 
     long long sn = 0, s1 = 0, s2 = 0;
     constexpr int NXC = N / 2;          // nx_corr = 2 xsearch = npx / 2
     constexpr int GU = 8;               // loads in flight per thread and operand
-    const int ntot = P.ny_corr * NXC;   // a multiple of NT * GU (ny_corr >= 64, NXC >= 64)
+    const int ntot = P.ny_corr * NXC;   // a multiple of NT * GU for windows of 64 and more
     for (int i0 = threadIdx.x; i0 < ntot; i0 += NT * GU) {
         float va[GU], vb[GU];
 #pragma unroll
         for (int u = 0; u < GU; u++) {
             const int i = i0 + u * NT;
             const int r = i / NXC, cc = i - r * NXC;
-            va[u] = __ldg(a1 + (size_t)r * N + cc);
-            vb[u] = __ldg(a2 + i);
+            // 32 x 32 windows (1024 samples) fill only half of one NT x GU pass
+            const bool in = (NXC >= 64) || (i < ntot);
+            va[u] = in ? __ldg(a1 + (size_t)r * N + cc) : m1f;
+            vb[u] = in ? __ldg(a2 + i) : m2f;
         }
 #pragma unroll
         for (int u = 0; u < GU; u++) {
@@ -958,11 +963,14 @@ static size_t rows_smem() {
            (size_t)teams * (fft_padded_len(N) * sizeof(float2) + (2 * N + 32) * sizeof(float)) +
            (size_t)(128 / 32) * 2 * (ACC + 32) * sizeof(float);
 }
-template <int M>
+template <int M, int THR = 128>
 static size_t cols_smem(int) {
-    using G = ColsGeom<M>;
+    using G = ColsGeom<M, THR>;
     return G::TWL * sizeof(float2) + (size_t)2 * G::CP * G::CS * sizeof(float2) + 2 * sizeof(double);
 }
+// resident k_peak CTAs per SM for configuration cfg
+template <int N>
+constexpr int peak_minb(int cfg) { return (N <= 256) ? (cfg == 1 ? 3 : 4) : (N <= 512 ? 2 : 1); }
 template <int N>
 static size_t peak_smem() {
     constexpr int T = fft_lanes(N);
@@ -986,18 +994,29 @@ static cudaError_t setup_rows() {
 }
 template <int M>
 static cudaError_t setup_cols(int) {
-    // the attribute is per kernel, shared by every context: size it for the
-    // largest chunk count any patch width gives (npx <= 1024: nchunks <= M)
-    return cudaFuncSetAttribute(k_cols<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_smem<M>(M));
+    // the attribute is per kernel, shared by every context
+    cudaError_t e = cudaFuncSetAttribute(k_cols<M, 128, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)cols_smem<M, 128>(M));
+    if (!e) e = cudaFuncSetAttribute(k_cols<M, 256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cols_smem<M, 256>(M));
+    if (!e) e = cudaFuncSetAttribute(k_cols<M, 128, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cols_smem<M, 128>(M));
+    return e;
 }
 template <int N>
 static cudaError_t setup_peak() {
-    return cudaFuncSetAttribute(k_peak<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)peak_smem<N>());
+    cudaError_t e = cudaFuncSetAttribute(k_peak<N, peak_minb<N>(0)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)peak_smem<N>());
+    if (!e && peak_minb<N>(1) != peak_minb<N>(0))
+        e = cudaFuncSetAttribute(k_peak<N, peak_minb<N>(1)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)peak_smem<N>());
+    return e;
 }
 
 cudaError_t kernels_setup(const Plan &P) {
     cudaError_t e = cudaSuccess;
     switch (P.npx) {
+        case 64: e = setup_rows<64>(); if (!e) e = setup_peak<64>(); break;
         case 128: e = setup_rows<128>(); if (!e) e = setup_peak<128>(); break;
         case 256: e = setup_rows<256>(); if (!e) e = setup_peak<256>(); break;
         case 512: e = setup_rows<512>(); if (!e) e = setup_peak<512>(); break;
@@ -1006,6 +1025,7 @@ cudaError_t kernels_setup(const Plan &P) {
     }
     if (e) return e;
     switch (P.npy) {
+        case 64: e = setup_cols<64>(P.nchunks); break;
         case 128: e = setup_cols<128>(P.nchunks); break;
         case 256: e = setup_cols<256>(P.nchunks); break;
         case 512: e = setup_cols<512>(P.nchunks); break;
@@ -1031,17 +1051,26 @@ static void launch_rows_t(const Plan &P, cudaStream_t s) {
 }
 template <int M>
 static void launch_cols_t(const Plan &P, cudaStream_t s) {
-    constexpr int CP = ColsGeom<M>::CP;
-    dim3 grid((P.npx / 2) / CP, P.nwin);
-    k_cols<M><<<grid, ColsGeom<M>::THREADS, cols_smem<M>(P.nchunks), s>>>(P);
+    // 256-thread CTAs take twice the column pairs: only where that divides npx/2
+    const bool wide = P.cols_cfg == 1 && ((P.npx / 2) % ColsGeom<M, 256>::CP) == 0;
+    if (wide) {
+        dim3 grid((P.npx / 2) / ColsGeom<M, 256>::CP, P.nwin);
+        k_cols<M, 256, 2><<<grid, 256, cols_smem<M, 256>(P.nchunks), s>>>(P);
+        return;
+    }
+    dim3 grid((P.npx / 2) / ColsGeom<M>::CP, P.nwin);
+    if (P.cols_cfg == 2) k_cols<M, 128, 1><<<grid, 128, cols_smem<M>(P.nchunks), s>>>(P);
+    else k_cols<M, 128, 2><<<grid, 128, cols_smem<M>(P.nchunks), s>>>(P);
 }
 template <int N>
 static void launch_peak_t(const Plan &P, cudaStream_t s) {
-    k_peak<N><<<P.nwin, 256, peak_smem<N>(), s>>>(P);
+    if (P.peak_cfg == 1) k_peak<N, peak_minb<N>(1)><<<P.nwin, 256, peak_smem<N>(), s>>>(P);
+    else k_peak<N, peak_minb<N>(0)><<<P.nwin, 256, peak_smem<N>(), s>>>(P);
 }
 
 void launch_rows(const Plan &P, cudaStream_t s) {
     switch (P.npx) {
+        case 64: launch_rows_t<64>(P, s); break;
         case 128: launch_rows_t<128>(P, s); break;
         case 256: launch_rows_t<256>(P, s); break;
         case 512: launch_rows_t<512>(P, s); break;
@@ -1050,6 +1079,7 @@ void launch_rows(const Plan &P, cudaStream_t s) {
 }
 void launch_cols(const Plan &P, cudaStream_t s) {
     switch (P.npy) {
+        case 64: launch_cols_t<64>(P, s); break;
         case 128: launch_cols_t<128>(P, s); break;
         case 256: launch_cols_t<256>(P, s); break;
         case 512: launch_cols_t<512>(P, s); break;
@@ -1058,6 +1088,7 @@ void launch_cols(const Plan &P, cudaStream_t s) {
 }
 void launch_peak(const Plan &P, cudaStream_t s) {
     switch (P.npx) {
+        case 64: launch_peak_t<64>(P, s); break;
         case 128: launch_peak_t<128>(P, s); break;
         case 256: launch_peak_t<256>(P, s); break;
         case 512: launch_peak_t<512>(P, s); break;

@@ -193,8 +193,8 @@ extern "C" xcg_status xcg_correlate_device_noalloc(const xcg_params *p,
         return fail(XCG_ERR_ARG, "null buffer or empty image");
     const int xs = p->xsearch, ys = p->ysearch;
     auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
-    if (!pow2(xs) || !pow2(ys) || xs < 32 || ys < 32 || xs > 256 || ys > 256)
-        return fail(XCG_ERR_ARG, "xsearch/ysearch must be powers of two in 32..256");
+    if (!pow2(xs) || !pow2(ys) || xs < 16 || ys < 16 || xs > 256 || ys > 256)
+        return fail(XCG_ERR_ARG, "xsearch/ysearch must be powers of two in 16..256");
     if (p->nx_corr != 2 * xs || p->ny_corr != 2 * ys)
         return fail(XCG_ERR_UNSUPPORTED, "nx_corr/ny_corr must be 2*xsearch/2*ysearch");
     if (!(p->ri == 1 || p->ri == 2 || p->ri == 4 || p->ri == 8)) return fail(XCG_ERR_ARG, "ri must be 1, 2, 4 or 8");

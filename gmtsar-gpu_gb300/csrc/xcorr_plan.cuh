@@ -35,6 +35,9 @@ struct Plan {
     // precision form: the correlation's row/column DFTs as split-FP16
     // tensor-core matmuls (tc_dft.cu); 0 = FP32 SIMT FFTs
     int tc_form;
+    // launch shapes (xcorr_kernels.cu): k_cols 0 default, 1 256-thread CTAs, 2
+    // one staging group; k_peak 0 four CTAs/SM, 1 three
+    int cols_cfg, peak_cfg;
     const uint8_t *tc_a_row;   // prepared forward DFT operand for the rows (npx)
     const uint8_t *tc_a_col;   // forward DFT operand for the columns (npy)
     const uint8_t *tc_a_inv;   // inverse DFT rows of the surface band (nyc x npy)

@@ -88,14 +88,22 @@ static xcg_status get_bucket(xcg_stack *st, int xs, int ys, Bucket **out) {
     b.xs = xs; b.ys = ys;
     XCG_TRY(xcg_create(&p, st->device, 0, &b.ctx));
     XCG_TRY(ck(cudaEventCreateWithFlags(&b.staged, cudaEventDisableTiming), "cudaEventCreate"));
-    // an autotuned batch size for this geometry, if the cache file has one
+    // autotuned settings for this geometry, if the cache file has them: lines
+    // "npx npy ri interp_factor batch [cols_cfg peak_cfg]", the last matching
+    // line winning
     const char *cache = getenv("XCG_TUNE_CACHE");
     if (cache) {
         FILE *f = fopen(cache, "r");
         if (f) {
-            int a, bb, r, i, bt;
-            while (fscanf(f, "%d %d %d %d %d", &a, &bb, &r, &i, &bt) == 5)
-                if (a == 4 * xs && bb == 4 * ys && r == p.ri && i == p.interp_factor) b.batch = bt;
+            char line[256];
+            while (fgets(line, sizeof line, f)) {
+                int a, bb, r, i, bt, cc = 0, pc = 0;
+                const int n = sscanf(line, "%d %d %d %d %d %d %d", &a, &bb, &r, &i, &bt, &cc, &pc);
+                if (n < 5 || a != 4 * xs || bb != 4 * ys || r != p.ri || i != p.interp_factor) continue;
+                b.batch = bt;
+                b.ctx->base.cols_cfg = (n >= 7 && cc >= 0 && cc <= 2) ? cc : 0;
+                b.ctx->base.peak_cfg = (n >= 7 && pc >= 0 && pc <= 1) ? pc : 0;
+            }
             fclose(f);
         }
     }
@@ -250,6 +258,8 @@ void xcg_stack_get_stats(const xcg_stack *st, xcg_stack_stats *out) {
         out->bucket_npx[k] = 4 * st->buckets[k].xs;
         out->bucket_npy[k] = 4 * st->buckets[k].ys;
         out->bucket_batch[k] = st->buckets[k].batch > 0 ? st->buckets[k].batch : st->buckets[k].ctx->max_batch;
+        out->bucket_cols_cfg[k] = st->buckets[k].ctx->base.cols_cfg;
+        out->bucket_peak_cfg[k] = st->buckets[k].ctx->base.peak_cfg;
     }
 }
 
@@ -298,7 +308,10 @@ xcg_status xcg_stack_run(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, v
     return enqueue(st, s);
 }
 
-// Pick each bucket's windows per batch by timing candidates on these pairs.
+// Pick each bucket's windows per batch and launch shapes by timing
+// candidates on these pairs: batch sizes first (default shapes), then the
+// column stage's shape (columns per CTA, staging depth), then the peak
+// stage's residency, each keeping the best so far.
 xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, void *stream) {
     if (!st || npairs <= 0 || !pairs) return XCG_ERR_ARG;
     XCG_TRY(ck(cudaSetDevice(st->device), "cudaSetDevice"));
@@ -318,16 +331,11 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
         for (int i = 0; i < npairs; i++)
             if (pairs[i].xsearch == b.xs && pairs[i].ysearch == b.ys) { mine.push_back(pairs[i]); nwin += pairs[i].nlocs; }
         if (nwin == 0) continue;
-        std::vector<int> cands;
-        for (int c : {128, 256, 512, 1024, 2048, 4096})
-            if (c < b.ctx->max_batch && c < nwin) cands.push_back(c);
-        cands.push_back(std::min(b.ctx->max_batch, std::max(nwin, 1)));
-        float best = 1e30f;
-        int bestc = cands.back();
-        for (int c : cands) {
-            b.batch = c;
+        xcg::Plan &B = b.ctx->base;
+        // time the bucket's pairs with the current settings: one warm run, two timed
+        auto time_it = [&](float *out) -> xcg_status {
             XCG_TRY(plan_run(st, mine.data(), (int)mine.size()));
-            XCG_TRY(enqueue(st, s));                       // warm
+            XCG_TRY(enqueue(st, s));
             float tot = 0.f;
             for (int rep = 0; rep < 2; rep++) {
                 XCG_TRY(plan_run(st, mine.data(), (int)mine.size()));
@@ -339,12 +347,46 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
                 XCG_TRY(ck(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime"));
                 tot += ms;
             }
-            if (tot < best) { best = tot; bestc = c; }
+            *out = tot;
+            return XCG_OK;
+        };
+        B.cols_cfg = 0;
+        B.peak_cfg = 0;
+        std::vector<int> cands;
+        for (int c : {128, 256, 512, 1024, 2048, 4096})
+            if (c < b.ctx->max_batch && c < nwin) cands.push_back(c);
+        cands.push_back(std::min(b.ctx->max_batch, std::max(nwin, 1)));
+        float best = 1e30f;
+        int bestc = cands.back();
+        for (int c : cands) {
+            b.batch = c;
+            float t;
+            XCG_TRY(time_it(&t));
+            if (t < best) { best = t; bestc = c; }
         }
         b.batch = bestc;
+        int best_cols = 0, best_peak = 0;
+        for (int cfg = 1; cfg <= 2; cfg++) {
+            B.cols_cfg = cfg;
+            float t;
+            XCG_TRY(time_it(&t));
+            if (t < best) { best = t; best_cols = cfg; }
+        }
+        B.cols_cfg = best_cols;
+        B.peak_cfg = 1;
+        {
+            float t;
+            XCG_TRY(time_it(&t));
+            if (t < best) { best = t; best_peak = 1; }
+        }
+        B.peak_cfg = best_peak;
         if (cache) {
             FILE *f = fopen(cache, "a");
-            if (f) { fprintf(f, "%d %d %d %d %d\n", 4 * b.xs, 4 * b.ys, st->common.ri, st->common.interp_factor, bestc); fclose(f); }
+            if (f) {
+                fprintf(f, "%d %d %d %d %d %d %d\n", 4 * b.xs, 4 * b.ys, st->common.ri, st->common.interp_factor, bestc,
+                        best_cols, best_peak);
+                fclose(f);
+            }
         }
     }
     cudaEventDestroy(e0);

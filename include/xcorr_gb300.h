@@ -36,7 +36,8 @@ typedef enum {
 /* Correlation parameters (struct xcorr fields, xcorr.h:19-63, with the
  * defaults of set_defaults, parse_xcorr_input.c:38-88). */
 typedef struct {
-    int32_t xsearch, ysearch;   /* search half-widths, powers of two in 32..256 (default 64) */
+    int32_t xsearch, ysearch;   /* search half-widths, powers of two in 16..256 (default 64); 16 (windows of
+                                   32) in the frequency-domain mode only */
     int32_t nx_corr, ny_corr;   /* correlation window; the reference ties them to 2*xsearch, 2*ysearch */
     int32_t ri;                 /* range interpolation factor: 1 (-norange), 2 (default), 4 or 8 */
     int32_t interp_flag;        /* 1: subpixel refinement (default); 0: -nointerp */
@@ -181,6 +182,9 @@ typedef struct {
     int64_t windows, launches, graph_replays, last_graph_launches;
     int32_t batches, last_graph_batches, buckets, pad;
     int32_t bucket_npx[8], bucket_npy[8], bucket_batch[8];
+    int32_t bucket_cols_cfg[8];  /* column-stage launch shape: 0 128-thread CTAs, two cp.async staging groups;
+                                    1 256-thread CTAs; 2 one staging group */
+    int32_t bucket_peak_cfg[8];  /* peak-stage residency: 0 four CTAs per SM, 1 three */
 } xcg_stack_stats;
 
 typedef struct xcg_stack xcg_stack;
@@ -197,8 +201,11 @@ xcg_status xcg_stack_run(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, v
  * graph on `stream` (not the legacy stream); later runs with identical pairs
  * and locations replay it. */
 void xcg_stack_set_graph(xcg_stack *st, int32_t enable);
-/* Time candidate batch sizes per bucket on these pairs and keep the fastest
- * (appended to the file named by XCG_TUNE_CACHE, read back by new buckets). */
+/* Time candidates per bucket on these pairs and keep the fastest: windows per
+ * batch, then the column stage's launch shape (column pairs per CTA, cp.async
+ * staging depth), then the peak stage's residency (appended to the file named
+ * by XCG_TUNE_CACHE as "npx npy ri interp_factor batch cols_cfg peak_cfg",
+ * read back by new buckets). */
 xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, void *stream);
 void xcg_stack_get_stats(const xcg_stack *st, xcg_stack_stats *out);
 

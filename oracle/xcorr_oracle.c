@@ -134,10 +134,23 @@ static double half_block_sum(const double *x)
     return s[0];
 }
 
+/* Surfaces that are a whole number of 2048-element blocks (every window of
+ * 64 or more) are summed block by block as above.  A 32 x 32 surface (1024
+ * elements) is less than one block: reduce6 zero-pads the elements past n,
+ * but h_reduce_strip computes its block count as n / 2048 = 0 and launches
+ * nothing (conv_ampl_demean.cu:645,660), so the reference has no value
+ * there; this restatement takes the zero-padded block reduce6 would have
+ * reduced, the sum of elements [0, 512) of the partial block. */
 static double xo_half_sum_ref(const double *x, int64_t n)
 {
     double acc = 0.0;
-    for (int64_t b0 = 0; b0 + 2048 <= n; b0 += 2048) acc += half_block_sum(x + b0);
+    int64_t b0 = 0;
+    for (; b0 + 2048 <= n; b0 += 2048) acc += half_block_sum(x + b0);
+    if (b0 < n) {
+        double pad[2048] = {0};
+        memcpy(pad, x + b0, sizeof(double) * (size_t)(n - b0));
+        acc += half_block_sum(pad);
+    }
     return acc;
 }
 
@@ -269,7 +282,9 @@ int xo_run(const xo_params *p, int precision, int format,
            xo_result *out)
 {
     if (!p || !out || nlocs < 0) return 1;
-    if ((p->npx * p->npy) % 1024 || ((int64_t)p->nxc * p->nyc) % 2048) return 2;
+    /* patches are whole 1024-sample reduction blocks; a 32 x 32 surface is half
+     * of one 2048-element argmax block (see xo_half_sum_ref) */
+    if ((p->npx * p->npy) % 1024 || ((int64_t)p->nxc * p->nyc) % 1024) return 2;
     prewarm(p);
     const int n2 = p->n2x * p->n2y;
     double *mds = (double *)calloc((size_t)nlocs * n2 + 1, sizeof(double));

@@ -54,7 +54,8 @@ def test_struct_layouts_match_header(tmp_path):
 
 def test_create_rejects_bad_parameters_without_touching_the_gpu():
     # argument validation happens before any device call
-    for kw in (dict(xsearch=48), dict(xsearch=16), dict(ri=3), dict(interp_factor=12), dict(corr_mode=3)):
+    for kw in (dict(xsearch=48), dict(xsearch=8), dict(ri=3), dict(interp_factor=12), dict(corr_mode=3),
+               dict(xsearch=16, corr_mode=0)):
         p = xg.params(**kw)
         with pytest.raises(xg.XcgError) as e:
             xg.Context(p)

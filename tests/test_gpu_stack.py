@@ -117,5 +117,65 @@ def test_autotune_and_split_strips(tmp_path, monkeypatch):
     for it, a in zip(items, alone):
         if it["nxl"] <= 7:
             _same(_host(it["dr"]), a)
-    assert len(cache.read_text().splitlines()) >= 1 + 4
+    lines = cache.read_text().splitlines()
+    assert len(lines) >= 1 + 4 and all(len(l.split()) == 7 for l in lines[1:])
+    s = st.stats()
+    assert all(0 <= s.bucket_cols_cfg[i] <= 2 and 0 <= s.bucket_peak_cfg[i] <= 1 for i in range(s.buckets))
+    st.close()
+
+
+def test_stack_every_bucket_against_oracle():
+    """One stack holding windows of 32, 64, 128 and 256 (xsearch 16 to 128,
+    one bucket each, pairs of different sizes, offsets and stretch): every
+    window against the oracle's FP32 restatement of the reference path,
+    integer and subpixel peaks identical, correlation within 1e-4."""
+    torch = pytest.importorskip("torch")
+    import xcorr_oracle as xo
+    dev = torch.device("cuda", 0)
+    spec = [(768, 768, 1.6, -0.8, 16, 16, 6, 4, 0, 0, 0.0),
+            (1024, 1024, -2.2, 1.3, 32, 32, 4, 3, 3, -2, 5e-4),
+            (1536, 1536, 0.7, 2.6, 64, 64, 3, 2, 0, 0, 0.0),
+            (2560, 2560, -1.9, -3.3, 128, 128, 2, 2, 0, 0, 0.0)]
+    items = []
+    for i, (nx, ny, dx, dy, xs, ys, nxl, nyl, xoff, yoff, ast) in enumerate(spec):
+        m, s = synth.make_pair(synth.PairSpec(nx=nx, ny=ny, dx=dx, dy=dy, noise_frac=0.1, seed=300 + i))
+        locs = xg.grid(nx, ny, nxl, nyl, xs, ys)
+        items.append(dict(m=m, s=s, locs=locs, xs=xs, ys=ys, nxl=nxl, xo=xoff, yo=yoff, ast=ast,
+                          dm=torch.from_numpy(m).to(dev), ds=torch.from_numpy(s).to(dev),
+                          dr=torch.zeros((len(locs), xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)))
+    st = xg.Stack(xg.params())
+    st.run(_pairs(items), 0)
+    torch.cuda.synchronize()
+    assert st.stats().buckets == 4
+    for it in items:
+        got = _host(it["dr"])
+        o = xo.run(xo.params(it["xs"], it["ys"]), it["m"], it["s"], it["locs"], it["xo"], it["yo"], it["ast"],
+                   precision=xo.F32, strip_len=it["nxl"])
+        for k in ("ip", "jp", "fip", "fjp", "flags"):
+            np.testing.assert_array_equal(got[k], o[k], err_msg=f"window {2 * it['xs']}: {k}")
+        rel = np.abs(got["gamma"] - o["gamma"]) / np.abs(o["gamma"])
+        assert rel.max() < 1e-4, (it["xs"], rel.max())
+    st.close()
+
+
+@pytest.mark.parametrize("cols_cfg,peak_cfg", [(1, 0), (2, 1), (1, 1)])
+def test_tuned_launch_shapes_give_identical_results(tmp_path, monkeypatch, cols_cfg, peak_cfg):
+    """Every launch shape the autotuner chooses between (256-thread column
+    CTAs, one cp.async staging group, three peak CTAs per SM) computes the
+    same transforms in the same order: results bit-identical to the default."""
+    torch = pytest.importorskip("torch")
+    items = _setup(torch)
+    alone = [_alone(it) for it in items]
+    cache = tmp_path / "tune.txt"
+    cache.write_text("".join(f"{4 * xs} {4 * ys} 2 16 0 {cols_cfg} {peak_cfg}\n"
+                             for xs, ys in {(it["xs"], it["ys"]) for it in items}))
+    monkeypatch.setenv("XCG_TUNE_CACHE", str(cache))
+    st = xg.Stack(xg.params())
+    st.run(_pairs(items), 0)
+    torch.cuda.synchronize()
+    s = st.stats()
+    assert [s.bucket_cols_cfg[i] for i in range(s.buckets)] == [cols_cfg] * s.buckets
+    assert [s.bucket_peak_cfg[i] for i in range(s.buckets)] == [peak_cfg] * s.buckets
+    for it, a in zip(items, alone):
+        _same(_host(it["dr"]), a)
     st.close()
