@@ -5,17 +5,19 @@ images made of independent 256 x 256 speckle tiles, each with its own
 (slave) shift -- a random integer part in [-4, 4] px plus a subpixel part
 uniform in [-0.5, 0.5] px in each axis -- and its own SNR, uniform in
 0..30 dB.  One window sits on each tile (128x128 windows, 256x256 patches,
-range interpolation 2, as the 128^2-window configuration).  The plain path
-returns each window's normalised 9x9 peak neighbourhood (the refiner's input)
-and its integer offset; the target is the subpixel position of the true peak
-in surface pixels, fx = xoff - ri*dx, fy = yoff - dy, the quantities
-highres_corr estimates as xfrac/yfrac.
+as the 128^2-window configuration), with range interpolation 2 (the
+reference's default, refiner/subpix_refiner.f32) or 1 (no range
+interpolation: the surrogate form, refiner/subpix_refiner_ri1.f32).  The plain
+path returns each window's normalised 9x9 peak neighbourhood (the refiner's
+input) and its integer offset; the target is the subpixel position of the
+true peak in surface pixels, fx = xoff - ri*dx, fy = yoff - dy, the
+quantities highres_corr estimates as xfrac/yfrac.
 
 Every network computation (forward, backward, Adam, inference) runs in the
 library's CUDA kernels; torch only supplies device memory and the random
 tiles.
 
-    python -m xcorr_gb300.refiner_train --windows 2000000 --out <dir>
+    python -m xcorr_gb300.refiner_train --windows 2000000 [--ri 1] --out <dir>
 """
 from __future__ import annotations
 
@@ -30,9 +32,18 @@ import numpy as np
 import xcorr_gb300 as xg
 
 TILE = 256
-RI = 2
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.dirname(HERE)), "refiner", "subpix_refiner.f32")
+REFINER_DIR = os.path.join(os.path.dirname(os.path.dirname(HERE)), "refiner")
+DEFAULT_WEIGHTS = os.path.join(REFINER_DIR, "subpix_refiner.f32")
+
+
+def weights_name(ri: int) -> str:
+    """File name of the trained parameters for surfaces of range interpolation ri."""
+    return "subpix_refiner.f32" if ri == 2 else f"subpix_refiner_ri{ri}.f32"
+
+
+def weights_path(ri: int) -> str:
+    return os.path.join(REFINER_DIR, weights_name(ri))
 
 
 def load_weights(path: str = DEFAULT_WEIGHTS) -> np.ndarray:
@@ -104,23 +115,23 @@ def plain_windows(ctx, master, slave, locs, device):
     return r, feat
 
 
-def targets(r, shift):
-    fx = r["xoff"].astype(np.float64) - RI * shift[:, 0]
+def targets(r, shift, ri):
+    fx = r["xoff"].astype(np.float64) - ri * shift[:, 0]
     fy = r["yoff"].astype(np.float64) - shift[:, 1]
     return np.stack([fx, fy], axis=1).astype(np.float32)
 
 
-def dataset(nwin: int, seed: int, device, tiles_side: int = 32):
+def dataset(nwin: int, seed: int, device, tiles_side: int = 32, ri: int = 2):
     """nwin training windows: features (torch), targets (torch), plain results, shifts."""
     import torch
-    ctx = xg.Context(xg.params(TILE // 4, TILE // 4, RI, 1, 16), device=device.index)
+    ctx = xg.Context(xg.params(TILE // 4, TILE // 4, ri, 1, 16), device=device.index)
     feats, tgts, plains, shifts, snrs = [], [], [], [], []
     per = tiles_side * tiles_side
     for i in range((nwin + per - 1) // per):
         m, s, locs, sh, snr = make_tiles(tiles_side, tiles_side, seed * 100003 + i, device)
         r, f = plain_windows(ctx, m, s, locs, device)
         feats.append(f)
-        tgts.append(torch.from_numpy(targets(r, sh)).to(device))
+        tgts.append(torch.from_numpy(targets(r, sh, ri)).to(device))
         plains.append(r)
         shifts.append(sh)
         snrs.append(snr)
@@ -129,7 +140,7 @@ def dataset(nwin: int, seed: int, device, tiles_side: int = 32):
             np.concatenate(shifts)[:nwin], np.concatenate(snrs)[:nwin])
 
 
-def evaluate(ref, feat, tgt, plain, device, max_sigma=0.15, max_dis=0.25):
+def evaluate(ref, feat, tgt, plain, device, max_sigma=0.15, max_dis=0.25, ri=2):
     """Errors of the refiner, of the plain FFT interpolation and of the combined
     rule (refiner where confident, plain elsewhere), in original pixels (the
     range axis divided by the range interpolation factor), on windows whose
@@ -158,8 +169,8 @@ def evaluate(ref, feat, tgt, plain, device, max_sigma=0.15, max_dis=0.25):
 
     def rms(a, b):
         d = (a - b)[good]
-        return dict(x=float(np.sqrt(np.mean((d[:, 0] / RI) ** 2))), y=float(np.sqrt(np.mean(d[:, 1] ** 2))))
-    return dict(windows=int(n), within_one_px=int(good.sum()), refiner_used=float(use[good].mean()),
+        return dict(x=float(np.sqrt(np.mean((d[:, 0] / ri) ** 2))), y=float(np.sqrt(np.mean(d[:, 1] ** 2))))
+    return dict(windows=int(n), range_interp=ri, within_one_px=int(good.sum()), refiner_used=float(use[good].mean()),
                 sigma_quantiles=[float(q) for q in np.quantile(sg[good], [0.1, 0.5, 0.9])],
                 max_sigma=max_sigma, max_disagree=max_dis,
                 rms_vs_truth_px=dict(refiner=rms(o[:, :2], t), fft_interp=rms(pl, t), combined=rms(mix, t)),
@@ -167,13 +178,13 @@ def evaluate(ref, feat, tgt, plain, device, max_sigma=0.15, max_dis=0.25):
 
 
 def train(nwin: int, steps_per_epoch: int | None = None, epochs: int = 12, batch: int = 4096, lr: float = 2e-3,
-          seed: int = 1, device=None, log=print, target: str = "truth"):
+          seed: int = 1, device=None, log=print, target: str = "truth", ri: int = 2):
     """target "truth": the generator's shift; "plain": the plain method's own
     subpixel answer (the network then stands in for the FFT interpolation)."""
     import torch
     device = device or torch.device("cuda", 0)
     t0 = time.time()
-    feat, tgt, plain, shift, snr = dataset(nwin, seed, device)
+    feat, tgt, plain, shift, snr = dataset(nwin, seed, device, ri=ri)
     hold = max(4096, nwin // 20)
     if target == "plain":
         import torch as _t
@@ -206,7 +217,7 @@ def train(nwin: int, steps_per_epoch: int | None = None, epochs: int = 12, batch
         log(f"epoch {ep + 1}/{epochs}: held-out loss {loss:.4f}")
     torch.cuda.synchronize(device)
     train_s = time.time() - t1
-    report = evaluate(ref, fte, tte, pte, device)
+    report = evaluate(ref, fte, tte, pte, device, ri=ri)
     report.update(train_windows=int(ntr), steps=step, batch=batch, train_seconds=train_s,
                   data_seconds=t1 - t0, seed=seed, target=target, epochs=epochs)
     return ref, report
@@ -218,11 +229,13 @@ def main():
     ap.add_argument("--epochs", type=int, default=12)
     ap.add_argument("--out", default=os.path.dirname(DEFAULT_WEIGHTS))
     ap.add_argument("--target", default="truth", choices=["truth", "plain"])
+    ap.add_argument("--ri", type=int, default=2, choices=[1, 2], help="range interpolation of the surfaces")
     a = ap.parse_args()
-    ref, report = train(a.windows, epochs=a.epochs, target=a.target)
+    ref, report = train(a.windows, epochs=a.epochs, target=a.target, ri=a.ri)
     os.makedirs(a.out, exist_ok=True)
-    ref.get_params().astype("<f4").tofile(os.path.join(a.out, "subpix_refiner.f32"))
-    with open(os.path.join(a.out, "train_report.json"), "w") as f:
+    ref.get_params().astype("<f4").tofile(os.path.join(a.out, weights_name(a.ri)))
+    rep_name = "train_report.json" if a.ri == 2 else f"train_report_ri{a.ri}.json"
+    with open(os.path.join(a.out, rep_name), "w") as f:
         json.dump(report, f, indent=1)
     print(json.dumps(report, indent=1))
 

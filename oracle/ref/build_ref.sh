@@ -7,7 +7,8 @@
 # and oracle/_ref/ref_host_probe, the reference's host C functions (PRM parse,
 # location grid, result writer) behind a small driver for CPU parity tests, and
 # oracle/_ref/ref_time_probe, the reference's do_time_corr (-time / -time4) on
-# supplied integer patches.
+# supplied integer patches, and oracle/_ref/xcorr-gb300-shim, the reference
+# program calling this library in place of its do_correlation.
 #
 # Two additions are needed for a current toolchain (both outside the sources):
 #   * oracle/ref/helper_cuda.h stands in for the CUDA-samples header named in gpu_err.h:9;
@@ -64,4 +65,22 @@ $NVCC "$OBJ/xcorr.o" "$OBJ/fft_interpolate_routines.o" "$OBJ/conv_ampl_demean.o"
 $NVCC "$OBJ/xcorr_dump.o" "$OBJ/fft_interpolate_routines.o" "$OBJ/conv_ampl_demean.o" "$OBJ/do_freq_xcorr_dump.o" \
       "$OBJ/do_time_int_xcorr.o" "$OBJ/highres_corr_dump.o" "$OBJ/dump_hooks.o" $LIBC "$OBJ/print_results_renamed.o" \
       -lm -lcufft -o "$OUT/xcorr-gpu-dump"
-echo "build_ref: built $OUT/xcorr-gpu $OUT/xcorr-gpu-dump $OUT/ref_host_probe $OUT/ref_time_probe"
+# the reference program with its do_correlation replaced by the library call
+# of gmtsar-gpu_gb300/integration/do_correlation_shim.cpp (the binding
+# INTEGRATION.md shows): xcorr.cu's host code compiled without inlining and
+# its do_correlation made a weak symbol, so main, set_defaults,
+# parse_command_line, handle_prm, get_locations and print_results are the
+# reference's own and main calls the shim's definition
+PKGDIR=$(cd "$HERE/../../gmtsar-gpu_gb300" && pwd)
+if [ -f "$PKGDIR/lib/libxcorr_gb300.so" ]; then
+  $NV -Xcompiler -O0 -Xcompiler -fno-inline -c "$REF/xcorr.cu" -o "$OBJ/xcorr_shimhost.o"
+  # do_correlation(struct xcorr) with C++ linkage, as xcorr.cu (CUDA C++) defines it
+  objcopy --weaken-symbol=_Z14do_correlation5xcorr "$OBJ/xcorr_shimhost.o"
+  ${CXX:-g++} -O2 -fcommon -w -I"$REF" -I"$PKGDIR/../include" -c "$PKGDIR/integration/do_correlation_shim.cpp" \
+      -o "$OBJ/do_correlation_shim.o"
+  $NVCC "$OBJ/xcorr_shimhost.o" "$OBJ/do_correlation_shim.o" "$OBJ/fft_interpolate_routines.o" \
+        "$OBJ/conv_ampl_demean.o" "$OBJ/do_freq_xcorr.o" "$OBJ/do_time_int_xcorr.o" "$OBJ/highres_corr.o" $LIBC \
+        "$OBJ/print_results.o" -L"$PKGDIR/lib" -lxcorr_gb300 -Xlinker -rpath -Xlinker "$PKGDIR/lib" -lm -lcufft \
+        -o "$OUT/xcorr-gb300-shim"
+fi
+echo "build_ref: built $OUT/xcorr-gpu $OUT/xcorr-gpu-dump $OUT/ref_host_probe $OUT/ref_time_probe $OUT/xcorr-gb300-shim"

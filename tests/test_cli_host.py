@@ -105,3 +105,12 @@ def test_missing_files_are_reported(tmp_path, cli):
     synth.write_prm(str(tmp_path / "aligned.PRM"), "nothere.SLC", 100, 100)
     p = _run(cli, str(tmp_path), [], {"XCORR_DRY_RUN": "1"})
     assert p.returncode == 1 and "Cannot open SLC_file" in p.stderr
+
+
+def test_integration_doc_shows_the_built_shim():
+    """INTEGRATION.md section 2 shows the shim that oracle/ref/build_ref.sh
+    builds and tests/test_gpu_shim.py runs, character for character."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    doc = open(os.path.join(root, "INTEGRATION.md")).read()
+    shim = open(os.path.join(root, "gmtsar-gpu_gb300", "integration", "do_correlation_shim.cpp")).read()
+    assert "```cpp\n" + shim + "```" in doc
