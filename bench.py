@@ -463,6 +463,10 @@ def surrogate_measure(dev, dm, ds, dl, locs, dr_plain, flush, stream, steps, war
                      "oracle's (= the plain form's) RMS error plus 0.02 px, per axis",
            "rms_px_vs_truth_plain": err_plain}
     forms = {}
+    # decision thresholds per form: refiner sigma below 0.15 px and agreement
+    # with a 3-point parabola within max_disagree; a parabola through 1-px
+    # samples (ri = 1) is biased by up to ~0.3 px, so that form allows 0.4
+    thresholds = {1: (0.15, 0.4), 2: (0.15, 0.25)}
     for ri in (1, 2):
         wpath = rt.weights_path(ri)
         if not os.path.exists(wpath):
@@ -475,7 +479,8 @@ def surrogate_measure(dev, dm, ds, dl, locs, dr_plain, flush, stream, steps, war
 
         def step():
             ctx.correlate_device_refined(ref, dm.data_ptr(), 2048, 4096, ds.data_ptr(), 2048, 4096, dl.data_ptr(),
-                                         nwin, drr.data_ptr(), sp, strip_len=20, max_sigma=0.15, max_disagree=0.25)
+                                         nwin, drr.data_ptr(), sp, strip_len=20, max_sigma=thresholds[ri][0],
+                                         max_disagree=thresholds[ri][1])
         ms = _device_steps(step, flush, stream, steps, warmup)
         rr = np.frombuffer(drr.cpu().numpy().tobytes(), dtype=xg.RESULT_DTYPE)
         xr_, yr_ = xg.output_offsets(rr, ri, 0, 0, locs[:, 1], 0.0)
@@ -484,7 +489,8 @@ def surrogate_measure(dev, dm, ds, dl, locs, dr_plain, flush, stream, steps, war
         forms[f"ri{ri}"] = {"value": v, "ms_per_step": ms / steps, "ratio_vs_plain": v / plain_value,
                             "refined_fraction": float(np.mean((rr["flags"] & xg.FLAG_REFINED) != 0)),
                             "rms_px_vs_truth": e, "rms_px_vs_plain": [rms(xr_ - xp_), rms(yr_ - yp_)],
-                            "within_target": bool(all(a <= b + 0.02 for a, b in zip(e, err_plain)))}
+                            "within_target": bool(all(a <= b + 0.02 for a, b in zip(e, err_plain))),
+                            "max_sigma": thresholds[ri][0], "max_disagree": thresholds[ri][1]}
         ctx.close()
         ref.close()
     out["forms"] = forms

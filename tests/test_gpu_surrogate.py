@@ -8,7 +8,9 @@ declines.
 * The plain form's offsets equal the FP64 oracle's on a 100-window sample, so
   the benchmark's "RMS against the plain form" is RMS against the FP64 oracle.
 * Declined windows are bit-identical to the plain ri = 1 path; refined ones
-  carry XCG_FLAG_REFINED.
+  carry XCG_FLAG_REFINED.  The refiner is taken where its sigma is below
+  0.15 px and it agrees with a 3-point parabola within 0.4 px (a parabola
+  through 1-px samples is biased by up to about 0.3 px).
 * The claimed reading of the benchmark spec's accuracy bar: per axis, the
   surrogate's RMS error against the synthetic truth is at most the FP64
   oracle's RMS error plus 0.02 px.
@@ -70,7 +72,7 @@ def test_surrogate_form_accuracy_and_fallback(cfg1):
         out = torch.zeros((n, xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
         ctx1.correlate_device_refined(ref, dm.data_ptr(), m.shape[1], m.shape[0], ds.data_ptr(), s.shape[1],
                                       s.shape[0], dl.data_ptr(), n, out.data_ptr(), sp, strip_len=20,
-                                      max_sigma=0.15, max_disagree=0.25)
+                                      max_sigma=0.15, max_disagree=0.4)
         torch.cuda.synchronize()
         ref.close()
     sur = np.frombuffer(out.cpu().numpy().tobytes(), dtype=xg.RESULT_DTYPE)
