@@ -33,7 +33,7 @@ def _cuda_home():
     return home
 
 
-CU_SOURCES = ["xcorr_kernels.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "xcorr_stack.cu", "refiner.cu", "refiner_api.cu", "fit_offsets.cu", "time_corr.cu", "tc_dft.cu", "peak_probe.cu"]
+CU_SOURCES = ["xcorr_kernels.cu", "xcorr_api.cu", "xcorr_noalloc.cu", "xcorr_stack.cu", "refiner.cu", "refiner_api.cu", "fit_offsets.cu", "time_corr.cu", "tc_dft.cu", "peak_probe.cu", "segment_rows.cu"]
 
 
 def _run(cmd):

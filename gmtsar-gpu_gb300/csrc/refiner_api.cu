@@ -10,6 +10,7 @@
 #include "refiner.cuh"
 #include "xcorr_ctx.cuh"
 #include "xcorr_gb300.h"
+#include "segment_rows.cuh"
 #include "xcorr_kernels.cuh"
 
 struct xcg_refiner {
@@ -197,13 +198,20 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *
         P.nwin = (nlocs - w0 < bw) ? nlocs - w0 : bw;
         P.locs = d_locs + w0;
         P.skip = nullptr;
-        xcg::launch_rows(P, s);
         if (P.tc_form) {                         // precision form: tensor-core DFT stages
+            P.rc = 0;
+            xcg::launch_rows(P, s);
             xcg::launch_tc_rows(P, s);
             xcg::launch_tc_cols(P, s);
             xcg::launch_tc_inv(P, s);
             c->stats.launches += 2;
+        } else if (P.rc) {                       // shared row segments
+            xcg::launch_rc_plan(P, s);
+            xcg::launch_segrows(P, s);
+            xcg::launch_cols_rc(P, s);
+            c->stats.launches += 1;
         } else {
+            xcg::launch_rows(P, s);
             xcg::launch_cols(P, s);
         }
         xcg::launch_peak(P, s);

@@ -1,0 +1,673 @@
+// Shared row segments: the row stage of the frequency-domain path computed
+// once per image row segment rather than once per window that reads it.
+//
+// Windows of one column of the location grid read the same columns of the
+// same image rows: with y_inc = 72 and 256-row patches (the 128 x 128
+// configuration) each master and slave row segment belongs to about 3.5
+// windows, with 512-row patches and y_inc = 74 (the full frame) to about 7.
+// The reference cuts, range-interpolates and transforms every window's
+// patch on its own (xcorr.cu:330-338, 237-292); the amplitudes of a row
+// segment do not depend on the window, so they are computed once here and
+// every window's means, (int) copies and time correlation see the same
+// numbers the per-window path computes.  The demean and mask enter in the
+// frequency domain by linearity (k_cols_rc), so the row spectra do not depend
+// on the window either.
+//
+//   k_rc_plan   one CTA per batch: every window contributes a master and a
+//               slave entry (pair, image, first column, first row); entries
+//               with the same pair, image, first column and first row modulo
+//               the rows of a chunk are sorted by row and merged where their
+//               row ranges overlap or touch; each merged run gets a range of
+//               1024-sample chunks, so a window's patch is a run of
+//               consecutive chunk rows
+//   k_segrows   one warp per chunk (rows per chunk = 1024 / npx): the patch
+//               rows of k_rows (read, range interpolation, amplitude, the
+//               reference's FP32 chunk sums, extremes, out-of-image flags),
+//               then the half spectra of the chunk's rows, two real rows per
+//               complex FFT separated by Hermitian symmetry
+//   k_cols_rc   per group of columns kx of one window: the column FFTs of
+//               the master's and the masked slave's half spectra, the
+//               product with the demean/mask corrections and the inverse
+//               column FFT of the surface rows, as k_cols
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "kernel_util.cuh"
+#include "segment_rows.cuh"
+#include "team_fft.cuh"
+
+namespace xcg {
+
+// ------------------------------------------------------------------ planner
+
+constexpr int RC_ENTRIES = 2 * RC_MAX_WINDOWS;   // sort capacity, a power of two
+constexpr int PLAN_THREADS = 1024;
+constexpr int PER_THREAD = RC_ENTRIES / PLAN_THREADS;
+// Sort key: pair (15 bits) | image (1) | first column + 2^19 (20) | first row
+// modulo the chunk rows (4) | first row + 2^23 (24).  The group of an entry is
+// the key without its low 24 bits.
+constexpr int KEY_Y_BITS = 24;
+constexpr int KEY_Y_BIAS = 1 << 23;
+constexpr int KEY_X_BIAS = 1 << 19;
+
+// In-place exclusive scan of a[0, RC_ENTRIES) by the whole CTA; returns the total.
+__device__ int block_exclusive_scan(int *a, int *wsum) {
+    const int t = threadIdx.x, l32 = t & 31, wp = t >> 5;
+    int v[PER_THREAD];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < PER_THREAD; k++) { v[k] = a[t * PER_THREAD + k]; s += v[k]; }
+    int inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (l32 >= o) inc += u;
+    }
+    if (l32 == 31) wsum[wp] = inc;
+    __syncthreads();
+    if (wp == 0) {
+        int x = (l32 < PLAN_THREADS / 32) ? wsum[l32] : 0;
+        int xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, xi, o);
+            if (l32 >= o) xi += u;
+        }
+        wsum[32 + l32] = xi - x;                  // exclusive prefix of the warp totals
+        if (l32 == 31) wsum[64] = xi;             // CTA total
+    }
+    __syncthreads();
+    int run = wsum[32 + wp] + inc - s;
+#pragma unroll
+    for (int k = 0; k < PER_THREAD; k++) { a[t * PER_THREAD + k] = run; run += v[k]; }
+    const int total = wsum[64];
+    __syncthreads();
+    return total;
+}
+
+__device__ __forceinline__ int key_y(unsigned long long k) {
+    return (int)(k & ((1ull << KEY_Y_BITS) - 1)) - KEY_Y_BIAS;
+}
+
+__global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
+    extern __shared__ unsigned long long plan_smem[];
+    unsigned long long *key = plan_smem;                        // [RC_ENTRIES] sort keys
+    int *pay = reinterpret_cast<int *>(key + RC_ENTRIES);      // [RC_ENTRIES] entry = 2 w + image
+    int *cnt = pay + RC_ENTRIES;                               // [RC_ENTRIES] run starts before each entry
+    int *rlen = cnt + RC_ENTRIES;                              // [RC_ENTRIES] chunks of each run, then its first chunk
+    int *rhead = rlen + RC_ENTRIES;                            // [RC_ENTRIES] first entry of each run
+    int *rtail = rhead + RC_ENTRIES;                           // [RC_ENTRIES] last entry of each run
+    int *wsum = rtail + RC_ENTRIES;                            // [72] scan scratch
+
+    const int tid = threadIdx.x;
+    const int nent = 2 * P.nwin;
+    const int npx = P.npx, npy = P.npy, rpc = P.rpc;
+    int n = 2;
+    while (n < nent) n <<= 1;
+    for (int e = tid; e < RC_ENTRIES; e += PLAN_THREADS) {
+        unsigned long long k = ~0ull;             // padding sorts last
+        if (e < nent) {
+            const int w = e >> 1, img = e & 1;
+            const xcg_loc loc = P.locs[w];
+            int local, pidx;
+            const PairDev pd = pair_of(P, w, local, pidx);
+            const int x0 = img ? loc.x + pd.x_offset - npx / 2 : loc.x - npx / 2;
+            const int y0 = img ? loc.y + pd.y_offset + slave_row_shift(pd, loc.y) - npy / 2 : loc.y - npy / 2;
+            const int ym = ((y0 % rpc) + rpc) % rpc;
+            k = ((unsigned long long)pidx << 49) | ((unsigned long long)img << 48) |
+                ((unsigned long long)(x0 + KEY_X_BIAS) << 28) | ((unsigned long long)ym << KEY_Y_BITS) |
+                (unsigned long long)(y0 + KEY_Y_BIAS);
+        }
+        key[e] = k;
+        pay[e] = e;
+        rlen[e] = 0;
+    }
+    __syncthreads();
+    // bitonic sort of the first n keys, payload alongside
+    for (int kk = 2; kk <= n; kk <<= 1) {
+        for (int j = kk >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < n; i += PLAN_THREADS) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = key[i], b = key[ixj];
+                    const bool up = (i & kk) == 0;
+                    if ((a > b) == up) {
+                        key[i] = b; key[ixj] = a;
+                        const int t = pay[i]; pay[i] = pay[ixj]; pay[ixj] = t;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // a run starts where the group changes or the next patch leaves a gap of rows
+    auto is_head = [&](int i) {
+        return i == 0 || (key[i] >> KEY_Y_BITS) != (key[i - 1] >> KEY_Y_BITS) || key_y(key[i]) > key_y(key[i - 1]) + npy;
+    };
+    for (int i = tid; i < RC_ENTRIES; i += PLAN_THREADS) cnt[i] = (i < nent && is_head(i)) ? 1 : 0;
+    __syncthreads();
+    const int nruns = block_exclusive_scan(cnt, wsum);
+    for (int i = tid; i < nent; i += PLAN_THREADS) {
+        const bool h = is_head(i);
+        const int r = cnt[i] + (h ? 0 : -1);
+        if (h) rhead[r] = i;
+        if (i == nent - 1 || is_head(i + 1)) rtail[r] = i;
+    }
+    __syncthreads();
+    // every patch spans npy rows, so a run ends npy rows below its last entry's first row
+    for (int r = tid; r < nruns; r += PLAN_THREADS)
+        rlen[r] = (key_y(key[rtail[r]]) - key_y(key[rhead[r]]) + npy) / rpc;
+    __syncthreads();
+    const int total = block_exclusive_scan(rlen, wsum);   // rlen[r] <- first chunk of run r
+    for (int i = tid; i < nent; i += PLAN_THREADS) {
+        const int r = cnt[i] + (is_head(i) ? 0 : -1);
+        const int c0 = rlen[r] + (key_y(key[i]) - key_y(key[rhead[r]])) / rpc;
+        reinterpret_cast<int *>(P.rc_wch)[pay[i]] = c0;   // rc_wch[w].x for the master, .y for the slave
+    }
+    // chunk descriptors, each chunk's run by binary search over the runs' first chunks
+    for (int c = tid; c < total; c += PLAN_THREADS) {
+        int lo = 0, hi = nruns - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (rlen[mid] <= c) lo = mid; else hi = mid - 1;
+        }
+        const unsigned long long k = key[rhead[lo]];
+        const int pidx = (int)(k >> 49), img = (int)((k >> 48) & 1);
+        const int x0 = (int)((k >> 28) & ((1u << 20) - 1)) - KEY_X_BIAS;
+        P.rc_desc[c] = make_int4(pidx, img, x0, key_y(k) + (c - rlen[lo]) * rpc);
+    }
+    if (tid == 0) *P.rc_count = total;
+}
+
+// ------------------------------------------------------------------ row stage
+
+// One warp per chunk of rows of one image segment; the structure of k_rows
+// (teams of T lanes, the rows t and t + 512 of the chunk through one team,
+// rows in registers in the team layout) with one image instead of a window's
+// two.  Range interpolation and amplitudes are k_rows' (xcorr.cu:237-250,
+// fft_interpolate_routines.cu:76-113, conv_ampl_demean.cu:98-108), the chunk
+// sum is h_reduceFD_strip's block sum (conv_ampl_demean.cu:703-726).
+template <int N, int LG>
+__global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_segrows(Plan P) {
+    constexpr int T = fft_lanes(N);
+    constexpr int TPW = 32 / T;
+    constexpr int PADN = fft_padded_len(N);
+    constexpr int RPC = (N >= 1024) ? 1 : 1024 / N;
+    constexpr int RPT = (N >= 1024) ? 1 : 2;
+    static_assert(RPT * TPW == RPC, "chunk rows");
+    constexpr int ACC = (N >= 1024) ? 1024 : 512;
+    constexpr int TWL = fft_twiddle_len(N);
+    constexpr int PER = N / T;
+    constexpr int NH = N / 2;
+    constexpr bool HSHIFT = (LG == 1) && (N <= 256);
+    constexpr int TWS = (N <= 256) ? 2 * TWL : TWL;
+    constexpr int RBP = 32;
+    constexpr int GOFF = 32 / TPW;
+
+    extern __shared__ float4 smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
+    const int lane = l32 % T;
+    const int tm = l32 / T;
+    const int team = warp * TPW + tm;
+    char *tbase = reinterpret_cast<char *>(tw + TWS) + (size_t)team * (PADN * sizeof(float2) + (2 * N + RBP) * sizeof(float));
+    float2 *ex = reinterpret_cast<float2 *>(tbase);
+    float *rb = reinterpret_cast<float *>(ex + PADN) + tm * GOFF;
+    const int rbx = tm & 1;
+    float *const rbE = rb + rbx, *const rbO = rb - rbx;
+    float *const rbL = (lane & 1) ? rbO : rbE;
+    float *acc = reinterpret_cast<float *>(reinterpret_cast<char *>(tw + TWS) +
+                                           (size_t)(blockDim.x / T) * (PADN * sizeof(float2) + (2 * N + RBP) * sizeof(float))) +
+                 (size_t)warp * (ACC + RBP);           // [ACC + RBP] first-level sums of the warp's chunk
+
+    for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_row[i];
+    if constexpr (HSHIFT)
+        for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[TWL + i] = P.phase[i];
+    __syncthreads();
+
+    constexpr int ri = 1 << LG;
+    constexpr int KM0 = (LG == 0) ? 0 : PER / (2 * ri), KM1 = (LG == 0) ? PER : 3 * PER / (2 * ri);
+    const int total = *P.rc_count;
+    const bool iq16 = (P.format == 0);
+
+    // chunks are taken four per CTA, one per warp; warps share no state
+    // between chunks, so a warp that runs out leaves without a barrier
+    for (int c = 4 * blockIdx.x + warp; c < total; c += 4 * gridDim.x) {
+        const int4 d = P.rc_desc[c];
+        const int img = d.y;
+        const PairDev *q = P.pairs ? P.pairs + d.x : nullptr;
+        const void *base = q ? (img ? q->slave : q->master) : (img ? P.single.slave : P.single.master);
+        const int nx = q ? (img ? q->s_nx : q->m_nx) : (img ? P.single.s_nx : P.single.m_nx);
+        const int ny = q ? (img ? q->s_ny : q->m_ny) : (img ? P.single.s_ny : P.single.m_ny);
+        const int x0 = d.z, y0 = d.w;
+        bool oob = false;
+        float mn = INFINITY, mx = -INFINITY;
+
+        auto load_row = [&](int r, uint32_t *raw) {
+            const int y = y0 + r;
+            const bool rowok = (y >= 0 && y < ny);
+            const uint32_t *row = reinterpret_cast<const uint32_t *>(base) + (size_t)(rowok ? y : 0) * (size_t)nx;
+            if (rowok && x0 >= 0 && x0 + N <= nx) {
+#pragma unroll
+                for (int m = 0; m < PER; m++) raw[m] = __ldg(row + x0 + lane + T * m);
+            } else {
+#pragma unroll
+                for (int m = 0; m < PER; m++) {
+                    const int x = x0 + lane + T * m;
+                    if (rowok && x >= 0 && x < nx) raw[m] = __ldg(row + x);
+                    else { raw[m] = 0u; oob = true; }
+                }
+            }
+        };
+        auto to_complex = [&](const uint32_t *raw, float2 *v) {
+            if (iq16) {
+#pragma unroll
+                for (int m = 0; m < PER; m++) {
+                    const short lo = (short)(raw[m] & 0xffffu), hi = (short)(raw[m] >> 16);
+                    v[m] = make_float2((float)lo, (float)hi);
+                }
+            } else {
+#pragma unroll
+                for (int m = 0; m < PER; m++) v[m] = make_float2(__uint_as_float(raw[m]), 0.f);
+            }
+        };
+        // amplitudes of one row into rb slot s (natural order of the kept fine samples)
+        auto amp_row = [&](int s, int r, const uint32_t *raw) {
+            float *const rowE = rbE + s * N, *const rowO = rbO + s * N;
+            float2 v[PER];
+            to_complex(raw, v);
+            if (LG == 0) {
+                float *const rowL = rbL + s * N;
+#pragma unroll
+                for (int m = 0; m < PER; m++) rowL[lane + T * m] = hypotf(v[m].x, v[m].y);
+                return;
+            }
+#pragma unroll
+            for (int m = KM0; m < KM1; m++) {
+                const int k = ((lane + T * m) << LG) - N / 2;
+                rowE[k] = amp_of(v[m]);
+            }
+#pragma unroll 1
+            for (int p = 1; p < ri; p++) {
+                if (p > 1) {
+                    uint32_t again[PER];
+                    load_row(r, again);
+                    to_complex(again, v);
+                }
+                team_fft_reg<N, -1>(v, ex, tw, lane);
+                if constexpr (HSHIFT) {
+                    team_ifft_half_shift<N>(v, ex, tw + TWL, lane);
+                } else {
+                    const float2 *ph = P.phase + (size_t)(p - 1) * N;
+#pragma unroll
+                    for (int m = 0; m < PER; m++) v[m] = cmulf(v[m], __ldg(ph + lane + T * m));
+                    team_fft_reg<N, +1>(v, ex, tw, lane);
+                }
+#pragma unroll
+                for (int m = KM0; m < KM1; m++) {
+                    const int k = ((lane + T * m) << LG) + p - N / 2;
+                    ((p & 1) ? rowO : rowE)[k] = amp_of(v[m]);
+                }
+            }
+        };
+
+        uint32_t raw[PER];
+        load_row(tm, raw);
+#pragma unroll 1
+        for (int ir = 0; ir < RPT; ir++) {
+            uint32_t cur[PER];
+#pragma unroll
+            for (int m = 0; m < PER; m++) cur[m] = raw[m];
+            if (ir + 1 < RPT) load_row((ir + 1) * TPW + tm, raw);     // in flight during this row
+            amp_row(ir, ir * TPW + tm, cur);
+        }
+        __syncwarp();
+        // amplitudes out, first reduction level (rows t and t + 512 of the
+        // chunk), extremes, and the FFT input: two real rows in one complex
+        // sequence; the slave's rows carry its mask columns [N/4, 3N/4) only
+        float *ag = P.rc_amp + (size_t)c * RPC * N;
+        float *acc1 = acc + tm * (N + GOFF);
+        float2 v[PER];
+#pragma unroll
+        for (int m = 0; m < PER; m++) {
+            const int e = lane + T * m;
+            const float a0 = rbL[e];
+            const float a1 = (RPT == 2) ? rbL[N + e] : 0.f;
+            const bool cin = (m >= PER / 4) && (m < 3 * PER / 4);
+            const bool use = (img == 0) || cin;
+            ag[(size_t)tm * N + e] = a0;
+            if (RPT == 2) ag[(size_t)(TPW + tm) * N + e] = a1;
+            acc1[e] = (RPT == 2) ? a0 + a1 : a0;
+            if (use) {
+                mn = fminf(mn, a0); mx = fmaxf(mx, a0);
+                if (RPT == 2) { mn = fminf(mn, a1); mx = fmaxf(mx, a1); }
+            }
+            v[m] = use ? make_float2(a0, a1) : make_float2(0.f, 0.f);
+        }
+        team_fft_reg<N, -1>(v, ex, tw, lane);
+        // half spectra k in [0, N/2) of both rows; bin 0 carries (DC, Nyquist),
+        // both real for a real row
+#pragma unroll
+        for (int m = 0; m < PER; m++) ex[fft_pad(lane + T * m)] = v[m];
+        __syncwarp();
+        float2 *s0 = P.rc_spec + ((size_t)c * RPC + tm) * NH;
+        float2 *s1 = P.rc_spec + ((size_t)c * RPC + TPW + tm) * NH;
+        const float2 xn = ex[fft_pad(N / 2)];
+#pragma unroll
+        for (int m = 0; m < PER / 2; m++) {
+            const int k = lane + T * m;
+            const float2 z1 = v[m];
+            if (RPT == 2) {
+                float2 A, B;
+                if (k == 0) {
+                    A = make_float2(z1.x, xn.x);
+                    B = make_float2(z1.y, xn.y);
+                } else {
+                    const float2 z2 = ex[fft_pad(N - k)];
+                    A = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+                    B = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+                }
+                s0[k] = A;
+                s1[k] = B;
+            } else {
+                s0[k] = (k == 0) ? make_float2(z1.x, xn.x) : z1;
+            }
+        }
+        __syncwarp();
+        oob = __ballot_sync(0xffffffffu, oob) != 0u;
+        // remaining tree levels, strides ACC/2 .. 1 (as k_rows)
+        {
+            float a[ACC / 32];
+#pragma unroll
+            for (int qq = 0; qq < ACC / 32; qq++) a[qq] = acc[l32 + 32 * qq + (32 * qq / N) * GOFF];
+#pragma unroll
+            for (int s = ACC / 64; s >= 1; s >>= 1)
+#pragma unroll
+                for (int qq = 0; qq < s; qq++) a[qq] = a[qq] + a[qq + s];
+            float x = a[0];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x = x + __shfl_xor_sync(0xffffffffu, x, o);
+            if (l32 == 0) P.rc_part[c] = x;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if (l32 == 0) {
+            P.rc_minmax[c] = make_float2(mn, mx);
+            P.rc_oob[c] = oob ? 1 : 0;
+        }
+        __syncwarp();        // acc and rb are reused by the warp's next chunk
+    }
+}
+
+// ------------------------------------------------------------------ column stage
+
+// k_cols on the cached half spectra: team kx transforms the master's and the
+// masked slave's column kx (rows of the window's chunks); kx = 0 holds the
+// packed (DC, Nyquist) columns, separated by Hermitian symmetry in ky.  The
+// product, demean/mask corrections (conv_ampl_demean.cu:111-139, applied by
+// linearity), (-1)^(kx+ky) shift and inverse column FFT of the surface rows
+// are k_cols' (do_freq_xcorr.cu:32-64, 106-114).
+template <int M, int THR>
+__global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan P) {
+    using G = ColsGeom<M, THR>;
+    constexpr int T = G::T, CS = G::CS, CP = G::CP, TWL = G::TWL;
+    constexpr int PER = M / T;
+    static_assert((CP & (CP - 1)) == 0 && T % 2 == 0, "columns per CTA: a power of two");
+
+    extern __shared__ float4 smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *cols = tw + TWL;                   // [2*CP + 1][CS]: master, slave, kx = N/2 product
+    float *shf = reinterpret_cast<float *>(cols + (2 * CP + 1) * CS);
+
+    const int w = blockIdx.y, b = blockIdx.x;
+    const int N = P.npx, NH = N / 2;
+    const int kx0 = b * CP;
+    const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
+    const int lane = l32 % T;
+    const int team = warp * (32 / T) + l32 / T;
+    const int2 wc = P.rc_wch[w];
+    const float2 *ms = P.rc_spec + (size_t)wc.x * P.rpc * NH;   // window's master rows, stride NH
+    const float2 *ss = P.rc_spec + (size_t)wc.y * P.rpc * NH;   // window's slave rows
+
+    for (int i = threadIdx.x; i < TWL; i += blockDim.x) tw[i] = P.tw_col[i];
+    {   // thread t stages slot t % CP for rows t / CP + k * THR/CP: the slave's
+        // mask rows [M/4, 3M/4) first (zeros elsewhere), then the master
+        constexpr int RSTEP = THR / CP;
+        constexpr int NLD = M / RSTEP;
+        const int sl = threadIdx.x % CP, row0 = threadIdx.x / CP;
+        float2 *sslot = cols + (CP + sl) * CS, *mslot = cols + sl * CS;
+#pragma unroll 8
+        for (int k = 0; k < NLD; k++) {
+            const int r = row0 + k * RSTEP;
+            if (r >= M / 4 && r < 3 * M / 4) cp_async8(sslot + fft_pad(r), ss + (size_t)r * NH + kx0 + sl);
+            else sslot[fft_pad(r)] = make_float2(0.f, 0.f);
+        }
+        cp_async_commit();
+#pragma unroll 8
+        for (int k = 0; k < NLD; k++) {
+            const int r = row0 + k * RSTEP;
+            cp_async8(mslot + fft_pad(r), ms + (size_t)r * NH + kx0 + sl);
+        }
+        cp_async_commit();
+    }
+    if (warp == 0) {
+        // patch means (conv_ampl_demean.cu:719-724): the FP32 chunk sums of a
+        // patch are exact in double, so any order gives the reference's bits
+        const int nch = P.nchunks;
+        double s1 = 0.0, s2 = 0.0;
+        for (int i = l32; i < nch; i += 32) { s1 += (double)P.rc_part[wc.x + i]; s2 += (double)P.rc_part[wc.y + i]; }
+        s1 = warp_sum_f64(s1);
+        s2 = warp_sum_f64(s2);
+        if (l32 == 0) {
+            const double inv = pow2_inv(N * M);
+            s1 *= inv;
+            s2 *= inv;
+            shf[0] = (float)(s1 * (double)N * (double)M);
+            shf[1] = (float)s2;
+            if (b == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
+        }
+    }
+    cp_async_wait<1>();                          // slave columns in (this thread's copies)
+    __syncthreads();                             // ... and everyone's
+    const float dc1 = shf[0];
+    const float m2 = shf[1];
+
+    const int kx = kx0 + team;
+    float2 *a = cols + team * CS;               // master column, later the result
+    float2 *pa = cols + (CP + team) * CS;       // slave column
+    float2 z[PER];
+#pragma unroll
+    for (int m = 0; m < PER; m++) z[m] = pa[fft_pad(lane + T * m)];
+    __syncwarp();
+    team_fft_reg<M, -1>(z, pa, tw, lane);
+#pragma unroll
+    for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
+    cp_async_wait<0>();                          // master columns in
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < PER; m++) z[m] = a[fft_pad(lane + T * m)];
+    __syncwarp();
+    team_fft_reg<M, -1>(z, a, tw, lane);
+#pragma unroll
+    for (int m = 0; m < PER; m++) a[fft_pad(lane + T * m)] = z[m];
+    __syncwarp();
+
+    // the kx = 0 team also emits column N/2 (its product goes through the
+    // extra slot first); the trip count stays warp-uniform because
+    // team_fft_reg synchronises the whole warp
+    const bool dc = (kx == 0);
+    const int nout = __any_sync(0xffffffffu, dc) ? 2 : 1;
+    float2 *xs = cols + 2 * CP * CS;
+    auto product = [&](int kxx, float2 A1, float2 A2, int ky) {
+        if (kxx == 0 && ky == 0) A1.x -= dc1;
+        const float2 bm = cmulf(__ldg(P.box_x + kxx), __ldg(P.box_y + ky));
+        A2.x -= m2 * bm.x;
+        A2.y -= m2 * bm.y;
+        float2 pr = cmulf_conj(A1, A2);
+        if ((kxx + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
+        return pr;
+    };
+#pragma unroll 1
+    for (int o = 0; o < nout; o++) {
+        if (o == 0) {
+#pragma unroll
+            for (int m = 0; m < PER; m++) {
+                const int ky = lane + T * m;
+                const float2 zm = a[fft_pad(ky)], zs = pa[fft_pad(ky)];
+                if (!dc) {
+                    z[m] = product(kx, zm, zs, ky);
+                } else {
+                    // columns kx = 0 and N/2 from the packed (DC, Nyquist) column
+                    const int kyn = (M - ky) & (M - 1);
+                    const float2 wm = a[fft_pad(kyn)], ws = pa[fft_pad(kyn)];
+                    const float2 D1 = make_float2(0.5f * (zm.x + wm.x), 0.5f * (zm.y - wm.y));
+                    const float2 D2 = make_float2(0.5f * (zs.x + ws.x), 0.5f * (zs.y - ws.y));
+                    const float2 Q1 = make_float2(0.5f * (zm.y + wm.y), -0.5f * (zm.x - wm.x));
+                    const float2 Q2 = make_float2(0.5f * (zs.y + ws.y), -0.5f * (zs.x - ws.x));
+                    z[m] = product(0, D1, D2, ky);
+                    xs[fft_pad(ky)] = product(NH, Q1, Q2, ky);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int m = 0; m < PER; m++) z[m] = xs[fft_pad(lane + T * m)];
+        }
+        float2 *dst = (o == 0) ? a : pa;
+        __syncwarp();                            // every lane has read a, pa and xs before dst is reused
+        team_fft_reg<M, +1>(z, dst, tw, lane);
+#pragma unroll
+        for (int m = PER / 4; m < 3 * PER / 4; m++) dst[fft_pad(lane + T * m)] = z[m];
+        __syncwarp();
+    }
+    __syncthreads();
+    // rows y in [ysearch, ysearch + nyc) of the half spectrum, kx <= N/2
+    {
+        constexpr int RS = THR / CP;
+        float2 *qw = P.qspec + (size_t)w * P.nyc * P.qpitch;
+        const int s = threadIdx.x % CP, y0 = threadIdx.x / CP;
+        float2 *dstq = qw + (size_t)y0 * P.qpitch + kx0 + s;
+        const float2 *srcc = cols + s * CS;
+        for (int k = 0; k < (M / 2) / RS; k++) {
+            const int sy = (RS % 16 == 0) ? fft_pad(y0 + M / 4) + k * (RS + RS / 16) : fft_pad(y0 + M / 4 + k * RS);
+            dstq[(size_t)k * RS * P.qpitch] = srcc[sy];
+        }
+        if (b == 0)                                // column N/2: the kx = 0 team's slave slot
+            for (int yq = threadIdx.x; yq < M / 2; yq += blockDim.x)
+                qw[(size_t)yq * P.qpitch + NH] = cols[CP * CS + fft_pad(yq + M / 4)];
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+
+static size_t rc_plan_smem_bytes() {
+    return (size_t)RC_ENTRIES * (sizeof(unsigned long long) + 5 * sizeof(int)) + 72 * sizeof(int);
+}
+template <int N>
+static size_t segrows_smem() {
+    constexpr int T = fft_lanes(N);
+    constexpr int ACC = (N >= 1024) ? 1024 : 512;
+    const int teams = 128 / T;
+    return fft_twiddle_len(N) * (N <= 256 ? 2 : 1) * sizeof(float2) +
+           (size_t)teams * (fft_padded_len(N) * sizeof(float2) + (2 * N + 32) * sizeof(float)) +
+           (size_t)(128 / 32) * (ACC + 32) * sizeof(float);
+}
+template <int M>
+static size_t cols_rc_smem() {
+    using G = ColsGeom<M, 128>;
+    return G::TWL * sizeof(float2) + (size_t)(2 * G::CP + 1) * G::CS * sizeof(float2) + 2 * sizeof(double);
+}
+
+template <int N>
+static cudaError_t setup_segrows_t() {
+    cudaError_t e = cudaSuccess;
+    auto set = [&](auto kern) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)segrows_smem<N>());
+    };
+    set(k_segrows<N, 0>); set(k_segrows<N, 1>); set(k_segrows<N, 2>); set(k_segrows<N, 3>);
+    return e;
+}
+template <int M>
+static cudaError_t setup_cols_rc_t() {
+    return cudaFuncSetAttribute(k_cols_rc<M, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_rc_smem<M>());
+}
+
+cudaError_t segrows_setup(const Plan &P) {
+    cudaError_t e = cudaFuncSetAttribute(k_rc_plan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rc_plan_smem_bytes());
+    if (e) return e;
+    switch (P.npx) {
+        case 64: e = setup_segrows_t<64>(); break;
+        case 128: e = setup_segrows_t<128>(); break;
+        case 256: e = setup_segrows_t<256>(); break;
+        case 512: e = setup_segrows_t<512>(); break;
+        case 1024: e = setup_segrows_t<1024>(); break;
+        default: return cudaErrorInvalidValue;
+    }
+    if (e) return e;
+    switch (P.npy) {
+        case 64: return setup_cols_rc_t<64>();
+        case 128: return setup_cols_rc_t<128>();
+        case 256: return setup_cols_rc_t<256>();
+        case 512: return setup_cols_rc_t<512>();
+        case 1024: return setup_cols_rc_t<1024>();
+    }
+    return cudaErrorInvalidValue;
+}
+
+size_t rc_max_chunks(int npx, int npy, int nwin) {
+    const int rpc = npx >= 1024 ? 1 : 1024 / npx;
+    return (size_t)2 * nwin * (size_t)(npy / rpc);
+}
+
+void launch_rc_plan(const Plan &P, cudaStream_t s) {
+    k_rc_plan<<<1, PLAN_THREADS, rc_plan_smem_bytes(), s>>>(P);
+}
+
+template <int N>
+static void launch_segrows_t(const Plan &P, cudaStream_t s) {
+    // a grid-stride walk over the planned chunks, four per CTA; the grid is
+    // sized for the chunks the batch would have without sharing, capped at
+    // the CTAs that fit the GPU at once several times over
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t maxq = (rc_max_chunks(P.npx, P.npy, P.nwin) + 3) / 4;
+    const int per_sm = (N >= 1024) ? 2 : (N >= 512 ? 3 : 4);
+    const int grid = (int)((maxq < (size_t)sms * per_sm * 8) ? maxq : (size_t)sms * per_sm * 8);
+    switch (P.log2ri) {
+        case 0: k_segrows<N, 0><<<grid, 128, segrows_smem<N>(), s>>>(P); break;
+        case 1: k_segrows<N, 1><<<grid, 128, segrows_smem<N>(), s>>>(P); break;
+        case 2: k_segrows<N, 2><<<grid, 128, segrows_smem<N>(), s>>>(P); break;
+        default: k_segrows<N, 3><<<grid, 128, segrows_smem<N>(), s>>>(P); break;
+    }
+}
+void launch_segrows(const Plan &P, cudaStream_t s) {
+    switch (P.npx) {
+        case 64: launch_segrows_t<64>(P, s); break;
+        case 128: launch_segrows_t<128>(P, s); break;
+        case 256: launch_segrows_t<256>(P, s); break;
+        case 512: launch_segrows_t<512>(P, s); break;
+        case 1024: launch_segrows_t<1024>(P, s); break;
+    }
+}
+
+template <int M>
+static void launch_cols_rc_t(const Plan &P, cudaStream_t s) {
+    constexpr int CP = ColsGeom<M, 128>::CP;
+    dim3 grid((P.npx / 2) / CP, P.nwin);
+    k_cols_rc<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
+}
+void launch_cols_rc(const Plan &P, cudaStream_t s) {
+    switch (P.npy) {
+        case 64: launch_cols_rc_t<64>(P, s); break;
+        case 128: launch_cols_rc_t<128>(P, s); break;
+        case 256: launch_cols_rc_t<256>(P, s); break;
+        case 512: launch_cols_rc_t<512>(P, s); break;
+        case 1024: launch_cols_rc_t<1024>(P, s); break;
+    }
+}
+
+}  // namespace xcg

@@ -21,6 +21,7 @@
 #include "xcorr_gb300.h"
 #include "time_corr.cuh"
 #include "xcorr_kernels.cuh"
+#include "segment_rows.cuh"
 #include "xcorr_ctx.cuh"
 
 using cd = std::complex<double>;
@@ -147,6 +148,10 @@ static size_t per_window_bytes(const xcg::Plan &B) {
     s += align256((size_t)B.nyc * B.qpitch * sizeof(float2));
     s += align256((size_t)B.nyc * B.nxc * sizeof(float));
     s += align256(64 * sizeof(float)) + align256(64) + align256(sizeof(double));
+    // shared row segments: at most 2 * nchunks chunks per window
+    const size_t ch = (size_t)2 * B.nchunks;
+    s += align256(ch * sizeof(int4)) + align256(sizeof(int2)) + align256(sizeof(int)) + align256(ch * 1024 * sizeof(float)) +
+         align256(ch * 512 * sizeof(float2)) + align256(ch * sizeof(float)) + align256(ch * sizeof(float2)) + align256(ch);
     return s;
 }
 
@@ -202,6 +207,8 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
     B.corr_mode = p->corr_mode;
     B.nchunks = B.npx * B.npy / 1024;
     B.qpitch = B.npx / 2 + 16;
+    B.rpc = B.npx >= 1024 ? 1 : 1024 / B.npx;
+    B.rc = (B.corr_mode == 2) ? 1 : 0;      // the frequency-domain mode shares row segments by default
 
     // tables
     std::vector<float2> tw_row = stockham_twiddles(B.npx), tw_col = stockham_twiddles(B.npy);
@@ -234,6 +241,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         B.kx = c->d_tables + o_kx;
         B.ky = c->d_tables + o_ky;
         XCG_CK_C(xcg::kernels_setup(B), "kernel attributes");
+        XCG_CK_C(xcg::segrows_setup(B), "kernel attributes");
         if (B.corr_mode < 2) XCG_CK_C(xcg::time_setup(B), "kernel attributes");
 
         // scratch: up to max_batch windows, at most 8 GiB or 40% of free memory
@@ -242,7 +250,8 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         XCG_CK_C(cudaMemGetInfo(&freeb, &totb), "cudaMemGetInfo");
         size_t budget = (size_t)8 << 30;
         if (budget > freeb * 2 / 5) budget = freeb * 2 / 5;
-        int mb = max_batch > 0 ? max_batch : 2048;
+        // at most RC_MAX_WINDOWS windows per batch: the row-segment planner's capacity
+        int mb = max_batch > 0 ? std::min(max_batch, xcg::RC_MAX_WINDOWS) : xcg::RC_MAX_WINDOWS;
         if ((size_t)mb * pw * c->nslots > budget) mb = (int)(budget / (pw * c->nslots));
         if (mb < 1) { st = XCG_ERR_NOMEM; g_last_error = "not enough device memory for one window"; goto fail; }
         c->max_batch = mb;
@@ -260,6 +269,15 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         c->off_md = take(64 * sizeof(float));
         c->off_mdnext = take(64);
         c->off_corr0n = take(sizeof(double));
+        const size_t ch = (size_t)2 * B.nchunks;        // chunks per window at most
+        c->off_rc_desc = take(ch * sizeof(int4));
+        c->off_rc_wch = take(sizeof(int2));
+        c->off_rc_count = take(sizeof(int));
+        c->off_rc_amp = take(ch * 1024 * sizeof(float));
+        c->off_rc_spec = take(ch * 512 * sizeof(float2));
+        c->off_rc_part = take(ch * sizeof(float));
+        c->off_rc_minmax = take(ch * sizeof(float2));
+        c->off_rc_oob = take(ch);
         c->slot_bytes = align256(off);
         c->scratch_bytes = c->slot_bytes * (size_t)c->nslots;
         XCG_CK_C(cudaMalloc(&c->d_scratch, c->scratch_bytes), "cudaMalloc scratch");
@@ -306,6 +324,12 @@ void xcg_destroy(xcg_ctx *c) {
     for (cudaEvent_t ev : c->band_ready) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+xcg_status xcg_set_row_sharing(xcg_ctx *c, int32_t enable) {
+    if (!c) return XCG_ERR_ARG;
+    c->base.rc = (enable && c->base.corr_mode == 2) ? 1 : 0;
+    return XCG_OK;
 }
 
 void xcg_set_features(xcg_ctx *c, float *d_features) {
@@ -368,6 +392,14 @@ Plan ctx_plan(const xcg_ctx *c) {
     P.md = (float *)(sc + c->off_md);
     P.mdnext = (unsigned char *)(sc + c->off_mdnext);
     P.corr0n = (double *)(sc + c->off_corr0n);
+    P.rc_desc = (int4 *)(sc + c->off_rc_desc);
+    P.rc_wch = (int2 *)(sc + c->off_rc_wch);
+    P.rc_count = (int *)(sc + c->off_rc_count);
+    P.rc_amp = (float *)(sc + c->off_rc_amp);
+    P.rc_spec = (float2 *)(sc + c->off_rc_spec);
+    P.rc_part = (float *)(sc + c->off_rc_part);
+    P.rc_minmax = (float2 *)(sc + c->off_rc_minmax);
+    P.rc_oob = (unsigned char *)(sc + c->off_rc_oob);
     return P;
 }
 
@@ -378,6 +410,8 @@ static Plan with_slot(Plan P, size_t off) {
     P.zrow = mv(P.zrow); P.amp1 = mv(P.amp1); P.amp2c = mv(P.amp2c); P.part = mv(P.part);
     P.oobmap = mv(P.oobmap); P.minmax = mv(P.minmax); P.means = mv(P.means); P.qspec = mv(P.qspec);
     P.surf = mv(P.surf); P.md = mv(P.md); P.mdnext = mv(P.mdnext); P.corr0n = mv(P.corr0n);
+    P.rc_desc = mv(P.rc_desc); P.rc_wch = mv(P.rc_wch); P.rc_count = mv(P.rc_count); P.rc_amp = mv(P.rc_amp);
+    P.rc_spec = mv(P.rc_spec); P.rc_part = mv(P.rc_part); P.rc_minmax = mv(P.rc_minmax); P.rc_oob = mv(P.rc_oob);
     return P;
 }
 
@@ -417,6 +451,10 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     // launch slots: rows, columns, peak, subpixel; the precision form splits
     // the column stage into three tensor-core DFT stages
     const bool tcf = P.tc_form != 0;
+    // shared row segments: frequency-domain FP32 path only (the precision
+    // form and the time modes read the per-window arrays)
+    if (tcf || P.corr_mode < 2) P.rc = 0;
+    const bool rc = P.rc != 0;
     const int nk = (tcf ? 6 : 4) - (P.interp_flag ? 0 : 1);
     if (c->profiling) {
         const size_t need = (size_t)nb * nk * 2;
@@ -468,8 +506,15 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
                 }
             } else {
                 switch (k) {
-                    case 0: launch_rows(Q, ss); break;
-                    case 1: if (tm) launch_tcorr(Q, ss); else launch_cols(Q, ss); break;
+                    case 0:
+                        if (rc) { launch_rc_plan(Q, ss); launch_segrows(Q, ss); c->stats.launches++; }
+                        else launch_rows(Q, ss);
+                        break;
+                    case 1:
+                        if (tm) launch_tcorr(Q, ss);
+                        else if (rc) launch_cols_rc(Q, ss);
+                        else launch_cols(Q, ss);
+                        break;
                     case 2: if (tm) launch_tpeak(Q, ss); else launch_peak(Q, ss); break;
                     case 3: launch_subpix(Q, ss); break;
                 }
@@ -579,6 +624,33 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     }
     size_t nev = 0;
     auto rows_hook = [&](const xcg::Plan &Q, cudaStream_t ss) -> xcg_status {
+        if (Q.rc) {
+            // shared row segments: the batch's rows are planned on the device,
+            // so its bands are copied first and the row stage waits for all of them
+            for (int k = 0; k < 2; k++) {
+                int lo, hi;
+                rows_of(Q.win0, Q.win0 + Q.nwin, k, lo, hi);
+                if (hi > done[k]) {
+                    XCG_CK(cudaMemcpyAsync((char *)c->d_img[k] + (size_t)done[k] * rowb[k],
+                                           (const char *)src[k] + (size_t)done[k] * rowb[k],
+                                           (size_t)(hi - done[k]) * rowb[k], cudaMemcpyHostToDevice, c->copy_stream),
+                           k ? "copy slave" : "copy master");
+                    done[k] = hi;
+                }
+            }
+            if (c->band_ready.size() <= nev) {
+                cudaEvent_t ev;
+                XCG_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+                c->band_ready.push_back(ev);
+            }
+            XCG_CK(cudaEventRecord(c->band_ready[nev], c->copy_stream), "cudaEventRecord");
+            XCG_CK(cudaStreamWaitEvent(ss, c->band_ready[nev], 0), "cudaStreamWaitEvent");
+            nev++;
+            xcg::launch_rc_plan(Q, ss);
+            xcg::launch_segrows(Q, ss);
+            c->stats.launches += 1;          // ctx_launch counts the row stage once
+            return XCG_OK;
+        }
         const int nsub = std::max(1, (Q.nwin + XCG_ROW_SUB / 2) / XCG_ROW_SUB);
         for (int j = 0; j < nsub; j++) {
             const int o0 = (int)((long long)Q.nwin * j / nsub), o1 = (int)((long long)Q.nwin * (j + 1) / nsub);

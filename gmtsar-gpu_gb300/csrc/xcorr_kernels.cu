@@ -22,17 +22,10 @@
 
 #include <type_traits>
 
+#include "kernel_util.cuh"
 #include "team_fft.cuh"
 #include "xcorr_kernels.cuh"
 
-// Launch shapes a plan selects (Plan::cols_cfg, Plan::peak_cfg; the stack's
-// autotuner times them per window geometry):
-//   k_cols  0: 128 threads, staging in two cp.async groups (partner columns
-//              first), 5 CTAs/SM (the default); 1: 256 threads (twice the
-//              column pairs per CTA), two groups; 2: 128 threads, one group
-//   k_peak  0: 4 resident CTAs/SM (64 registers, a few spills; beats 3 for
-//              transforms up to 256 points); 1: 3 CTAs/SM (85 registers)
-#define XCG_COLS_BLOCKS 5
 
 namespace xcg {
 
@@ -74,11 +67,6 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
     }
     return v;
 }
-__device__ __forceinline__ double warp_sum_f64(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 __device__ __forceinline__ long long warp_sum_i64(long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -95,31 +83,6 @@ __device__ __forceinline__ float2 load_sample(const Plan &P, const void *img, in
     return make_float2(__ldg(reinterpret_cast<const float *>(img) + i), 0.f);
 }
 
-// |v| of an interpolated sample.  The reference's amplitudes (hypotf of its
-// cuFFT outputs) and these (of this library's own FFT outputs) already differ
-// by transform rounding, so the hardware square root approximation
-// (sqrt.approx.f32) stands in for the correctly rounded sqrtf, whose
-// special-case branch cost k_rows 7% of its instructions.  Measured on GB300
-// against sqrtf: at most one unit in the last place (exhaustively over
-// [1, 4), so over every binade), equal on 83% of inputs, exact at zero.  The
-// flush-to-zero form drops the subnormal fix-up: a sum of squares below
-// 1.2e-38 (never negative) gives 0 instead of a value below 1.1e-19.
-__device__ __forceinline__ float amp_of(float2 v) {
-    const float s = fmaf(v.x, v.x, v.y * v.y);
-    float r;
-    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
-    return r;
-}
-
-// 1 / n for n a power of two, exactly (built from the exponent bits)
-__device__ __forceinline__ double pow2_inv(int n) {
-    const int lg = 31 - __clz(n);
-    return __longlong_as_double((long long)(1023 - lg) << 52);
-}
-
-__device__ __forceinline__ int slave_row_shift(const PairDev &pd, int y) {
-    return (int)((double)y * pd.astretcha);    // ishft, read_xcorr_data.c:65
-}
 
 // ---------------------------------------------------------------- k_rows
 // Replaces read_xcorr_data + the H2D patch cut (xcorr.cu:326-338), range
@@ -365,14 +328,6 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
     }
 }
 
-// ---------------------------------------------------------------- cp.async
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int NPEND>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND) : "memory"); }
 
 // ---------------------------------------------------------------- k_cols
 // Replaces the column half of the forward FFTs, d_mulaconjb/d_Cmul
@@ -385,17 +340,6 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // shared memory with coalesced row reads, each FFT uses its own column slot as
 // the exchange buffer (the column is in registers meanwhile), and the half
 // spectrum goes back row by row.
-template <int M, int THR = 128>
-struct ColsGeom {
-    static constexpr int T = fft_lanes(M);
-    static constexpr int PADM = fft_padded_len(M);
-    static constexpr int CS = PADM + 1;
-    static constexpr int THREADS = THR;
-    static constexpr int CP = THREADS / T;        // column pairs per CTA = teams
-    static constexpr int TWL = fft_twiddle_len(M);
-    static constexpr int BLOCKS = (M >= 1024) ? (THREADS >= 256 ? 1 : 2)
-                                : (M >= 512 ? (THREADS >= 256 ? 1 : 3) : XCG_COLS_BLOCKS * 128 / THREADS);
-};
 
 // DEPTH 2: partner and own columns staged as two cp.async groups, the partner
 // transforms overlapping the own columns' arrival; DEPTH 1: one group.
@@ -586,13 +530,30 @@ __global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
     // (its FFTs of zeros stay zeros); the packed transform here would leave
     // rounding residue of the other patch, so that case is set explicitly.
     if (warp == 0) {          // per-chunk extremes and out-of-image flags, reduced by one warp
-        const float *mm = P.minmax + (size_t)w * 4 * P.nchunks;
         float a = INFINITY, b = -INFINITY, c2 = INFINITY, d = -INFINITY;
         int oobf = 0;
-        for (int i = l32; i < P.nchunks; i += 32) {
-            a = fminf(a, mm[i]); b = fmaxf(b, mm[P.nchunks + i]);
-            c2 = fminf(c2, mm[2 * P.nchunks + i]); d = fmaxf(d, mm[3 * P.nchunks + i]);
-            oobf |= P.oobmap[(size_t)w * P.nchunks + i];
+        if (P.rc) {
+            // shared row segments: the window's chunks; the slave's extremes
+            // over the chunks of its mask rows (a chunk's rows are all inside
+            // or all outside: rows per chunk divide ysearch)
+            const int2 wc = P.rc_wch[w];
+            for (int i = l32; i < P.nchunks; i += 32) {
+                const float2 m1 = P.rc_minmax[wc.x + i];
+                a = fminf(a, m1.x); b = fmaxf(b, m1.y);
+                const int r0 = i * P.rpc;
+                if (r0 >= P.ysearch && r0 < M - P.ysearch) {
+                    const float2 m2 = P.rc_minmax[wc.y + i];
+                    c2 = fminf(c2, m2.x); d = fmaxf(d, m2.y);
+                }
+                oobf |= P.rc_oob[wc.x + i] | P.rc_oob[wc.y + i];
+            }
+        } else {
+            const float *mm = P.minmax + (size_t)w * 4 * P.nchunks;
+            for (int i = l32; i < P.nchunks; i += 32) {
+                a = fminf(a, mm[i]); b = fmaxf(b, mm[P.nchunks + i]);
+                c2 = fminf(c2, mm[2 * P.nchunks + i]); d = fmaxf(d, mm[3 * P.nchunks + i]);
+                oobf |= P.oobmap[(size_t)w * P.nchunks + i];
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -671,8 +632,20 @@ __global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
 
     // time-domain correlation at the integer peak on (int) demeaned amplitudes
     const float m1f = (float)P.means[2 * w], m2f = (float)P.means[2 * w + 1];
-    const float *a1 = P.amp1 + (size_t)w * M * N + (size_t)(P.ysearch + (int)ipeak) * N + (int)jpeak + P.xsearch;
-    const float *a2 = P.amp2c + (size_t)w * P.ny_corr * P.nx_corr;
+    // master patch rows (row stride N) and the slave's centre (row stride a2s):
+    // per window, or rows of the window's chunks of shared row segments
+    const float *a1, *a2;
+    int a2s;
+    if (P.rc) {
+        const int2 wc = P.rc_wch[w];
+        a1 = P.rc_amp + ((size_t)wc.x * P.rpc + P.ysearch + (int)ipeak) * N + (int)jpeak + P.xsearch;
+        a2 = P.rc_amp + ((size_t)wc.y * P.rpc + P.ysearch) * N + P.xsearch;
+        a2s = N;
+    } else {
+        a1 = P.amp1 + (size_t)w * M * N + (size_t)(P.ysearch + (int)ipeak) * N + (int)jpeak + P.xsearch;
+        a2 = P.amp2c + (size_t)w * P.ny_corr * P.nx_corr;
+        a2s = P.nx_corr;
+    }
     long long sn = 0, s1 = 0, s2 = 0;
     constexpr int NXC = N / 2;          // nx_corr = 2 xsearch = npx / 2
     constexpr int GU = 8;               // loads in flight per thread and operand
@@ -686,7 +659,7 @@ __global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
             // 32 x 32 windows (1024 samples) fill only half of one NT x GU pass
             const bool in = (NXC >= 64) || (i < ntot);
             va[u] = in ? __ldg(a1 + (size_t)r * N + cc) : m1f;
-            vb[u] = in ? __ldg(a2 + i) : m2f;
+            vb[u] = in ? __ldg(a2 + (size_t)r * a2s + cc) : m2f;
         }
 #pragma unroll
         for (int u = 0; u < GU; u++) {

@@ -78,6 +78,20 @@ struct Plan {
     unsigned char *mdnext;  // [nwin][n2y*n2x] 1 where the next window's value goes
     double *corr0n;   // [nwin]
     const unsigned char *skip;  // [nwin] 1: the subpixel stage leaves this window alone (null: none)
+
+    // shared row segments (segment_rows.cu): the row stage runs once per image
+    // row segment that one or more windows of the batch read, in chunks of
+    // 1024 samples; a window's patch rows are consecutive rows of its chunks
+    int rc;                 // 1: this path; 0: one row stage per window (zrow, amp1, ...)
+    int rpc;                // rows per chunk: 1024 / npx
+    int4 *rc_desc;          // [chunks] (pair, 0 master / 1 slave, first column, first row)
+    int2 *rc_wch;           // [nwin] first master (x) and slave (y) chunk of each window
+    int *rc_count;          // chunks of the batch (written by the planner)
+    float *rc_amp;          // [chunks][rpc][npx] amplitudes of the kept fine samples
+    float2 *rc_spec;        // [chunks][rpc][npx/2] half row spectra; bin 0 holds (DC, Nyquist)
+    float *rc_part;         // [chunks] FP32 chunk sums in the reference's tree order
+    float2 *rc_minmax;      // [chunks] (min, max); slave chunks over the mask columns only
+    unsigned char *rc_oob;  // [chunks] 1 where a sample lay outside its image
 };
 
 // The pair of batch window w (a copy: taking the address of the kernel

@@ -175,6 +175,8 @@ static xcg_status plan_run(xcg_stack *st, const xcg_pair *pairs, int npairs) {
     // batches: whole strips (of each pair) up to the batch size
     for (Bucket &b : st->buckets) {
         if (b.nwin == 0) continue;
+        // the row-segment planner keys pairs by a 15-bit index
+        if (b.npairs >= (1 << 15)) b.ctx->base.rc = 0;
         const int cap = (b.batch > 0 && b.batch <= b.ctx->max_batch) ? b.batch : b.ctx->max_batch;
         b.starts.push_back(0);
         int bstart = 0, w = 0;

@@ -28,7 +28,7 @@ EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_cre
            "xcg_refiner_destroy", "xcg_refiner_set_params", "xcg_refiner_get_params", "xcg_refiner_forward",
            "xcg_refiner_gradient", "xcg_refiner_train_step", "xcg_correlate_device_refined",
            "xcg_fit_offsets", "xcg_tc_gemm_check", "xcg_set_dft_form", "xcg_debug_inject_stage_timeout",
-           "xcg_fp32_fma_rate")
+           "xcg_fp32_fma_rate", "xcg_set_row_sharing")
 REFINER_NPARAM = 37507
 FLAG_REFINED = 4
 FLAG_STAGE_TIMEOUT = 8
@@ -163,6 +163,8 @@ def load(path: str | None = None):
     L.xcg_tc_gemm_check.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 4
     L.xcg_set_dft_form.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_debug_inject_stage_timeout.argtypes = [ctypes.c_void_p]
+    L.xcg_set_row_sharing.restype = ctypes.c_int
+    L.xcg_set_row_sharing.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_fp32_fma_rate.restype = ctypes.c_int
     L.xcg_fp32_fma_rate.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
@@ -218,6 +220,10 @@ class Context:
     def set_dft_form(self, form: int):
         """0: FP32 SIMT FFTs (default); 1: split-FP16 tensor-core DFTs (precision form)."""
         _check(self._L.xcg_set_dft_form(self._h, int(form)))
+
+    def set_row_sharing(self, on: bool):
+        """Row stage once per shared image row segment (default) or once per window."""
+        _check(self._L.xcg_set_row_sharing(self._h, 1 if on else 0))
 
     def inject_stage_timeout(self):
         """The next precision-form call behaves as if a tensor-core wait had run out (error-path tests)."""

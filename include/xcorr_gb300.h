@@ -209,6 +209,17 @@ void xcg_stack_set_graph(xcg_stack *st, int32_t enable);
 xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, void *stream);
 void xcg_stack_get_stats(const xcg_stack *st, xcg_stack_stats *out);
 
+/* Row stage of the frequency-domain FP32 path: 1 (the default) computes the
+ * range interpolation, amplitudes and row spectra once per image row segment
+ * that one or more windows of a batch read (windows of one column of the
+ * location grid share most of their rows) and gives every window a view of
+ * its rows; 0 computes them once per window, as the reference's
+ * do_correlation does (xcorr.cu:330-338 with d_assign_values, :237-292).
+ * Amplitudes, means and the time-domain correlation are the same bits either
+ * way; the spectra differ by FP32 rounding.  The precision form and the
+ * -time/-time4 modes always run the per-window row stage. */
+xcg_status xcg_set_row_sharing(xcg_ctx *ctx, int32_t enable);
+
 /* Make later xcg_correlate_device calls on this context also write, per
  * window, the 9x9 neighbourhood of the integer peak normalised by the surface
  * maximum (DEVICE [nlocs][81]; NULL stops it): the subpixel refiner's input. */
