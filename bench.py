@@ -60,6 +60,15 @@ def flops_per_window(npx=256, npy=256, ri=2):
             "k_peak": half, "k_subpix": sub}
 
 
+def row_flops(npx=256, ri=2):
+    """Algorithmic work of one patch row in the reference's count: range
+    interpolation (an npx-point forward and a ri*npx-point inverse FFT) and
+    the row half of the 2-D FFT (an npx-point FFT)."""
+    import math
+    f = lambda n: 5.0 * n * math.log2(n)
+    return 2 * f(npx) + (f(ri * npx) if ri > 1 else 0.0)
+
+
 def algorithmic_bytes_per_window(npx=256, npy=256):
     return 2 * npx * npy * 4       # both patches as complex int16
 
@@ -200,11 +209,11 @@ def cpu_baseline(m, s, locs, target_s=12.0):
                       "oracle FP32 restatement, OpenMP over windows"}
 
 
-def read_traffic():
-    """DRAM bytes per window of a k_rows launch, from the committed ncu
+def read_traffic(kernel="k_rows"):
+    """DRAM bytes per window of one launch of `kernel`, from its committed ncu
     summary (dram__bytes_read.sum + dram__bytes_write.sum of one captured
     launch divided by its windows), if any."""
-    path = os.path.join(ROOT, "profiles", "k_rows_256_500win.md")
+    path = os.path.join(ROOT, "profiles", f"{kernel}_256_500win.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -291,7 +300,9 @@ def frame_measure(steps, warmup, max_batch=0, e2e_calls=3):
             "config": {"workload": "full frame", "image": "10240x30720 complex int16, varying shift, 20 dB",
                        "windows": nwin, "xsearch": 128, "ysearch": 128, "range_interp": 2, "interp": 16,
                        "l2": "flushed between steps (256 MB write)", "generation_s": gen_s},
-            "kernel_ms_per_step": {n: st.kernel_ms[i] for i, n in enumerate(xg.KERNEL_NAMES)},
+            "kernel_ms_per_step": {n: st.kernel_ms[i] for i, n in
+                                   enumerate(xg.RC_KERNEL_NAMES if st.row_chunks > 0 else xg.KERNEL_NAMES)},
+            "row_chunks_per_step": int(st.row_chunks),
             "batches_per_step": st.batches,
             "e2e": {"value": nwin / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(m.nbytes + s.nbytes + locs.nbytes),
                     "d2h_bytes_per_step": int(nwin * xg.RESULT_DTYPE.itemsize),
@@ -601,15 +612,18 @@ def run_ours(args):
     ctx.set_profiling(True)
     kms = [0.0] * 4
     batches = 1
+    row_chunks = 0
     for _ in range(max(3, min(args.steps, 20))):
         flush.zero_()
         step()
         st = ctx.stats()
         batches = max(1, st.batches)
+        row_chunks += st.row_chunks
         for k in range(4):
             kms[k] += st.kernel_ms[k]
     ctx.set_profiling(False)
     nprof = max(3, min(args.steps, 20))
+    row_chunks /= nprof                 # 1024-sample chunks the row stage computed per step (0: per-window rows)
     # the FP32 SIMT ceiling of the roofline, measured on this GPU by the library's FMA kernel
     try:
         fma_tflops = xg.fp32_fma_rate(dev.index)
@@ -698,18 +712,31 @@ def run_ours(args):
         if os.path.exists(pk):
             peaks = _j.load(open(pk))
         fl = flops_per_window()
-        names = list(xg.KERNEL_NAMES)
+        shared = row_chunks > 0
+        names = list(xg.RC_KERNEL_NAMES if shared else xg.KERNEL_NAMES)
         dom = int(np.argmax(kms))
         dom_name = names[dom]
         # one launch per batch: the step's windows split into `batches` launches
         wpl = nwin / batches
         avg_ms = kms[dom] / nprof / batches
-        ach = fl[dom_name] * wpl / (avg_ms / 1e3) / 1e12
+        if dom_name == "k_segrows":
+            # the rows the launch computed: per unique row the reference's
+            # range interpolation (N-point forward, ri*N-point inverse) and row FFT
+            rows = row_chunks / batches * (1024 // 256)
+            flop_launch = rows * row_flops()
+            algo = (f"{row_flops() / 1e3:.1f} KFLOP per unique patch row x {rows:.0f} rows per launch "
+                    f"({row_chunks:.0f} chunks of 1024 samples per {nwin}-window step, {batches} launches; "
+                    f"{2 * nwin * 256:.0f} patch rows without sharing)")
+        else:
+            flop_launch = fl[dom_name.replace("_rc", "")] * wpl
+            algo = (f"{fl[dom_name.replace('_rc', '')] / 1e6:.2f} MFLOP/window x {wpl:.0f} windows per launch "
+                    f"({batches} launches per {nwin}-window step)")
+        ach = flop_launch / (avg_ms / 1e3) / 1e12
         smax = peaks.get("sm_max_mhz", 2070.0)
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         nominal = sms * 128 * 2 * smax * 1e6 / 1e12
         fp32_peak = fma_tflops if fma_tflops else nominal
-        tpw = read_traffic()
+        tpw = read_traffic(dom_name)
         traffic = tpw * wpl if tpw else None
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"bound": "fp32_simt", "kernel": dom_name, "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
@@ -719,8 +746,7 @@ def run_ours(args):
                                 f"lanes x 2 flop x {smax:.0f} MHz") if fma_tflops else
                                f"nominal FP32 SIMT rate, {sms} SMs x 128 lanes x 2 flop x {smax:.0f} MHz",
                 "fp32_nominal": nominal, "frac_of_nominal": ach / nominal,
-                "algorithmic": f"{fl[dom_name] / 1e6:.2f} MFLOP/window x {wpl:.0f} windows per launch "
-                               f"({batches} launches per {nwin}-window step)",
+                "algorithmic": algo, "row_chunks_per_step": row_chunks,
                 "avg_launch_ms": avg_ms,
                 "hbm": {"achieved": (traffic / (avg_ms / 1e3) / 1e9) if traffic else None, "peak": hbm_peak,
                         "unit": "GB/s", "frac": ((traffic / (avg_ms / 1e3) / 1e9) / hbm_peak) if traffic else None,

@@ -178,6 +178,33 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
         P.rc_desc[c] = make_int4(pidx, img, x0, key_y(k) + (c - rlen[lo]) * rpc);
     }
     if (tid == 0) *P.rc_count = total;
+    if (P.rc_nbands > 0) {
+        // counting sort of the chunks by row band (order within a band is free)
+        int *bcnt = wsum;                         // [0, 8) counts, [8, 16) fill, [16, 24) starts
+        const int nb = P.rc_nbands;
+        __syncthreads();                          // descriptors written; wsum free
+        if (tid < 32) wsum[tid] = 0;
+        __syncthreads();
+        auto band_of = [&](int c) {
+            const int4 d = P.rc_desc[c];
+            const int last = d.w + rpc - 1;
+            int b = 0;
+            while (b < nb - 1 && last >= P.rc_band_end[d.y][b]) b++;
+            return b;
+        };
+        for (int c = tid; c < total; c += PLAN_THREADS) atomicAdd(&bcnt[band_of(c)], 1);
+        __syncthreads();
+        if (tid == 0) {
+            int acc = 0;
+            for (int b = 0; b < nb; b++) { bcnt[16 + b] = acc; P.rc_band_start[b] = acc; acc += bcnt[b]; }
+            P.rc_band_start[nb] = acc;
+        }
+        __syncthreads();
+        for (int c = tid; c < total; c += PLAN_THREADS) {
+            const int b = band_of(c);
+            P.rc_order[bcnt[16 + b] + atomicAdd(&bcnt[8 + b], 1)] = c;
+        }
+    }
 }
 
 // ------------------------------------------------------------------ row stage
@@ -228,12 +255,16 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_s
 
     constexpr int ri = 1 << LG;
     constexpr int KM0 = (LG == 0) ? 0 : PER / (2 * ri), KM1 = (LG == 0) ? PER : 3 * PER / (2 * ri);
-    const int total = *P.rc_count;
+    // this launch's chunks: all of them in planned order, or one row band's
+    const bool banded = P.rc_nbands > 0;
+    const int begin = banded ? P.rc_band_start[P.rc_band] : 0;
+    const int end = banded ? P.rc_band_start[P.rc_band + 1] : *P.rc_count;
     const bool iq16 = (P.format == 0);
 
     // chunks are taken four per CTA, one per warp; warps share no state
     // between chunks, so a warp that runs out leaves without a barrier
-    for (int c = 4 * blockIdx.x + warp; c < total; c += 4 * gridDim.x) {
+    for (int i = begin + 4 * blockIdx.x + warp; i < end; i += 4 * gridDim.x) {
+        const int c = banded ? P.rc_order[i] : i;
         const int4 d = P.rc_desc[c];
         const int img = d.y;
         const PairDev *q = P.pairs ? P.pairs + d.x : nullptr;
@@ -636,7 +667,9 @@ static void launch_segrows_t(const Plan &P, cudaStream_t s) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const size_t maxq = (rc_max_chunks(P.npx, P.npy, P.nwin) + 3) / 4;
     const int per_sm = (N >= 1024) ? 2 : (N >= 512 ? 3 : 4);
-    const int grid = (int)((maxq < (size_t)sms * per_sm * 8) ? maxq : (size_t)sms * per_sm * 8);
+    // a band's launch takes a share of the chunks: a smaller grid
+    const size_t cap = (size_t)sms * per_sm * (P.rc_nbands > 0 ? 2 : 8);
+    const int grid = (int)((maxq < cap) ? maxq : cap);
     switch (P.log2ri) {
         case 0: k_segrows<N, 0><<<grid, 128, segrows_smem<N>(), s>>>(P); break;
         case 1: k_segrows<N, 1><<<grid, 128, segrows_smem<N>(), s>>>(P); break;

@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <stdint.h>
 
 #include <algorithm>
 #include <complex>
@@ -151,7 +152,8 @@ static size_t per_window_bytes(const xcg::Plan &B) {
     // shared row segments: at most 2 * nchunks chunks per window
     const size_t ch = (size_t)2 * B.nchunks;
     s += align256(ch * sizeof(int4)) + align256(sizeof(int2)) + align256(sizeof(int)) + align256(ch * 1024 * sizeof(float)) +
-         align256(ch * 512 * sizeof(float2)) + align256(ch * sizeof(float)) + align256(ch * sizeof(float2)) + align256(ch);
+         align256(ch * 512 * sizeof(float2)) + align256(ch * sizeof(float)) + align256(ch * sizeof(float2)) + align256(ch) +
+         align256(ch * sizeof(int)) + align256(sizeof(int));
     return s;
 }
 
@@ -278,6 +280,8 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         c->off_rc_part = take(ch * sizeof(float));
         c->off_rc_minmax = take(ch * sizeof(float2));
         c->off_rc_oob = take(ch);
+        c->off_rc_order = take(ch * sizeof(int));
+        c->off_rc_band_start = take(sizeof(int));       // 9 ints: one 256-byte block at least
         c->slot_bytes = align256(off);
         c->scratch_bytes = c->slot_bytes * (size_t)c->nslots;
         XCG_CK_C(cudaMalloc(&c->d_scratch, c->scratch_bytes), "cudaMalloc scratch");
@@ -400,6 +404,8 @@ Plan ctx_plan(const xcg_ctx *c) {
     P.rc_part = (float *)(sc + c->off_rc_part);
     P.rc_minmax = (float2 *)(sc + c->off_rc_minmax);
     P.rc_oob = (unsigned char *)(sc + c->off_rc_oob);
+    P.rc_order = (int *)(sc + c->off_rc_order);
+    P.rc_band_start = (int *)(sc + c->off_rc_band_start);
     return P;
 }
 
@@ -412,6 +418,7 @@ static Plan with_slot(Plan P, size_t off) {
     P.surf = mv(P.surf); P.md = mv(P.md); P.mdnext = mv(P.mdnext); P.corr0n = mv(P.corr0n);
     P.rc_desc = mv(P.rc_desc); P.rc_wch = mv(P.rc_wch); P.rc_count = mv(P.rc_count); P.rc_amp = mv(P.rc_amp);
     P.rc_spec = mv(P.rc_spec); P.rc_part = mv(P.rc_part); P.rc_minmax = mv(P.rc_minmax); P.rc_oob = mv(P.rc_oob);
+    P.rc_order = mv(P.rc_order); P.rc_band_start = mv(P.rc_band_start);
     return P;
 }
 
@@ -522,6 +529,12 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
             if (c->profiling) cudaEventRecord(c->events[ei++], ss);
             c->stats.launches++;
         }
+        if (c->profiling && rc) {     // the chunks this batch's row stage computed (profiling synchronises anyway)
+            int n = 0;
+            XCG_CK(cudaMemcpyAsync(&n, Q.rc_count, sizeof(int), cudaMemcpyDeviceToHost, ss), "read chunk count");
+            XCG_CK(cudaStreamSynchronize(ss), "cudaStreamSynchronize");
+            c->stats.row_chunks += n;
+        }
     }
     if (fork) {
         for (int k = 0; k < c->nslots; k++) {
@@ -625,30 +638,44 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     size_t nev = 0;
     auto rows_hook = [&](const xcg::Plan &Q, cudaStream_t ss) -> xcg_status {
         if (Q.rc) {
-            // shared row segments: the batch's rows are planned on the device,
-            // so its bands are copied first and the row stage waits for all of them
-            for (int k = 0; k < 2; k++) {
-                int lo, hi;
-                rows_of(Q.win0, Q.win0 + Q.nwin, k, lo, hi);
-                if (hi > done[k]) {
-                    XCG_CK(cudaMemcpyAsync((char *)c->d_img[k] + (size_t)done[k] * rowb[k],
-                                           (const char *)src[k] + (size_t)done[k] * rowb[k],
-                                           (size_t)(hi - done[k]) * rowb[k], cudaMemcpyHostToDevice, c->copy_stream),
-                           k ? "copy slave" : "copy master");
-                    done[k] = hi;
+            // shared row segments: the planner (which reads only the
+            // locations) orders the batch's chunks by row band of each image;
+            // band b's rows are copied, then its row-stage launch runs, so
+            // only the first band's copy is exposed
+            int lo[2], hi[2];
+            for (int k = 0; k < 2; k++) rows_of(Q.win0, Q.win0 + Q.nwin, k, lo[k], hi[k]);
+            xcg::Plan Qb = Q;
+            const int nb = std::max(1, std::min(8, Q.nwin / 128));
+            Qb.rc_nbands = nb;
+            for (int b = 0; b < nb; b++)
+                for (int k = 0; k < 2; k++)
+                    Qb.rc_band_end[k][b] = (b == nb - 1) ? INT32_MAX
+                                                         : lo[k] + (int)((long long)(hi[k] - lo[k]) * (b + 1) / nb);
+            xcg::launch_rc_plan(Qb, ss);
+            for (int b = 0; b < nb; b++) {
+                for (int k = 0; k < 2; k++) {
+                    const int end = std::min(hi[k], Qb.rc_band_end[k][b]);
+                    if (end > done[k]) {
+                        XCG_CK(cudaMemcpyAsync((char *)c->d_img[k] + (size_t)done[k] * rowb[k],
+                                               (const char *)src[k] + (size_t)done[k] * rowb[k],
+                                               (size_t)(end - done[k]) * rowb[k], cudaMemcpyHostToDevice,
+                                               c->copy_stream),
+                               k ? "copy slave" : "copy master");
+                        done[k] = end;
+                    }
                 }
+                if (c->band_ready.size() <= nev) {
+                    cudaEvent_t ev;
+                    XCG_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+                    c->band_ready.push_back(ev);
+                }
+                XCG_CK(cudaEventRecord(c->band_ready[nev], c->copy_stream), "cudaEventRecord");
+                XCG_CK(cudaStreamWaitEvent(ss, c->band_ready[nev], 0), "cudaStreamWaitEvent");
+                nev++;
+                Qb.rc_band = b;
+                xcg::launch_segrows(Qb, ss);
             }
-            if (c->band_ready.size() <= nev) {
-                cudaEvent_t ev;
-                XCG_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
-                c->band_ready.push_back(ev);
-            }
-            XCG_CK(cudaEventRecord(c->band_ready[nev], c->copy_stream), "cudaEventRecord");
-            XCG_CK(cudaStreamWaitEvent(ss, c->band_ready[nev], 0), "cudaStreamWaitEvent");
-            nev++;
-            xcg::launch_rc_plan(Q, ss);
-            xcg::launch_segrows(Q, ss);
-            c->stats.launches += 1;          // ctx_launch counts the row stage once
+            c->stats.launches += nb;          // the planner and the band launches; ctx_launch counts one
             return XCG_OK;
         }
         const int nsub = std::max(1, (Q.nwin + XCG_ROW_SUB / 2) / XCG_ROW_SUB);

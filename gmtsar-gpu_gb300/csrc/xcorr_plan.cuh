@@ -92,6 +92,14 @@ struct Plan {
     float *rc_part;         // [chunks] FP32 chunk sums in the reference's tree order
     float2 *rc_minmax;      // [chunks] (min, max); slave chunks over the mask columns only
     unsigned char *rc_oob;  // [chunks] 1 where a sample lay outside its image
+    // row bands (host entry): the planner also lists the chunks band by band,
+    // a chunk in the first band whose end row (per image) lies beyond the
+    // chunk's last row, so each band's row-stage launch can wait for its copy
+    int rc_nbands;          // 0: no band order, the row stage takes every chunk in planned order
+    int rc_band;            // with bands: this row-stage launch's band
+    int rc_band_end[2][8];  // master / slave rows [.., end) of each band
+    int *rc_order;          // [chunks] chunk indices band by band
+    int *rc_band_start;     // [9] first entry of each band in rc_order, then the total
 };
 
 // The pair of batch window w (a copy: taking the address of the kernel

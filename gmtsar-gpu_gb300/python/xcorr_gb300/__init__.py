@@ -57,10 +57,12 @@ RESULT_DTYPE = np.dtype([
 class Stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64), ("batches", ctypes.c_int32), ("batch_windows", ctypes.c_int32),
                 ("kernel_ms", ctypes.c_double * 8), ("scratch_bytes", ctypes.c_size_t),
-                ("nkernels", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("nkernels", ctypes.c_int32), ("pad", ctypes.c_int32), ("row_chunks", ctypes.c_int64)]
 
 
 KERNEL_NAMES = ("k_rows", "k_cols", "k_peak", "k_subpix")
+# launch slots with shared row segments: the planner and row kernel time together in slot 0
+RC_KERNEL_NAMES = ("k_segrows", "k_cols_rc", "k_peak", "k_subpix")
 TC_KERNEL_NAMES = ("k_rows", "k_tc_rows", "k_tc_cols", "k_tc_inv", "k_peak", "k_subpix")
 
 

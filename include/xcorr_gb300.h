@@ -91,6 +91,8 @@ typedef struct {
     size_t scratch_bytes;      /* device scratch held by the context */
     int32_t nkernels;          /* launch slots used in kernel_ms */
     int32_t pad;
+    int64_t row_chunks;        /* with profiling and shared row segments: 1024-sample chunks the row stage
+                                  computed (2 x nchunks per window without sharing) */
 } xcg_stats;
 
 const char *xcg_status_string(xcg_status s);
