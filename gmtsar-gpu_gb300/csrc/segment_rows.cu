@@ -367,8 +367,12 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_s
             const float a1 = (RPT == 2) ? rbL[N + e] : 0.f;
             const bool cin = (m >= PER / 4) && (m < 3 * PER / 4);
             const bool use = (img == 0) || cin;
-            ag[(size_t)tm * N + e] = a0;
-            if (RPT == 2) ag[(size_t)(TPW + tm) * N + e] = a1;
+            // the slave's amplitudes are read only inside its mask columns
+            // (the time-correlation window, [xsearch, xsearch + nx_corr))
+            if (use) {
+                ag[(size_t)tm * N + e] = a0;
+                if (RPT == 2) ag[(size_t)(TPW + tm) * N + e] = a1;
+            }
             acc1[e] = (RPT == 2) ? a0 + a1 : a0;
             if (use) {
                 mn = fminf(mn, a0); mx = fmaxf(mx, a0);
@@ -448,11 +452,14 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan 
     constexpr int T = G::T, CS = G::CS, CP = G::CP, TWL = G::TWL;
     constexpr int PER = M / T;
     static_assert((CP & (CP - 1)) == 0 && T % 2 == 0, "columns per CTA: a power of two");
+    static_assert(THR == 128, "four warps: two partial chunk sums per patch");
 
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *cols = tw + TWL;                   // [2*CP + 1][CS]: master, slave, kx = N/2 product
-    float *shf = reinterpret_cast<float *>(cols + (2 * CP + 1) * CS);
+    float2 *boxy = cols + (2 * CP + 1) * CS;    // [M] DFT of the row mask
+    float2 *boxx = boxy + M;                    // [CP + 1] DFT of the column mask at this CTA's kx, then N/2
+    double *dsum = reinterpret_cast<double *>(boxx + CP + 1);   // [4] per-warp partial chunk sums
 
     const int w = blockIdx.y, b = blockIdx.x;
     const int N = P.npx, NH = N / 2;
@@ -485,27 +492,31 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan 
         }
         cp_async_commit();
     }
-    if (warp == 0) {
-        // patch means (conv_ampl_demean.cu:719-724): the FP32 chunk sums of a
+    // the mask spectra this CTA uses, staged once (per-element reads missed
+    // the L1 left beside the column slots)
+    for (int i = threadIdx.x; i < M; i += THR) boxy[i] = __ldg(P.box_y + i);
+    if (threadIdx.x <= CP) boxx[threadIdx.x] = __ldg(P.box_x + (threadIdx.x < CP ? kx0 + threadIdx.x : NH));
+    {
+        // patch means (conv_ampl_demean.cu:719-724) from the chunk sums,
+        // warps 0-1 the master's, 2-3 the slave's: the FP32 chunk sums of a
         // patch are exact in double, so any order gives the reference's bits
         const int nch = P.nchunks;
-        double s1 = 0.0, s2 = 0.0;
-        for (int i = l32; i < nch; i += 32) { s1 += (double)P.rc_part[wc.x + i]; s2 += (double)P.rc_part[wc.y + i]; }
-        s1 = warp_sum_f64(s1);
-        s2 = warp_sum_f64(s2);
-        if (l32 == 0) {
-            const double inv = pow2_inv(N * M);
-            s1 *= inv;
-            s2 *= inv;
-            shf[0] = (float)(s1 * (double)N * (double)M);
-            shf[1] = (float)s2;
-            if (b == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
-        }
+        const int base = (warp < 2) ? wc.x : wc.y;
+        double sp = 0.0;
+        for (int i = (warp & 1) * 32 + l32; i < nch; i += 64) sp += (double)P.rc_part[base + i];
+        sp = warp_sum_f64(sp);
+        if (l32 == 0) dsum[warp] = sp;
     }
     cp_async_wait<1>();                          // slave columns in (this thread's copies)
     __syncthreads();                             // ... and everyone's
-    const float dc1 = shf[0];
-    const float m2 = shf[1];
+    float dc1, m2;
+    {
+        const double inv = pow2_inv(N * M);
+        const double s1 = (dsum[0] + dsum[1]) * inv, s2 = (dsum[2] + dsum[3]) * inv;
+        dc1 = (float)(s1 * (double)N * (double)M);   // the master's DC term, m1 N M
+        m2 = (float)s2;
+        if (b == 0 && threadIdx.x == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
+    }
 
     const int kx = kx0 + team;
     float2 *a = cols + team * CS;               // master column, later the result
@@ -535,7 +546,7 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan 
     float2 *xs = cols + 2 * CP * CS;
     auto product = [&](int kxx, float2 A1, float2 A2, int ky) {
         if (kxx == 0 && ky == 0) A1.x -= dc1;
-        const float2 bm = cmulf(__ldg(P.box_x + kxx), __ldg(P.box_y + ky));
+        const float2 bm = cmulf(boxx[kxx == NH ? CP : kxx - kx0], boxy[ky]);
         A2.x -= m2 * bm.x;
         A2.y -= m2 * bm.y;
         float2 pr = cmulf_conj(A1, A2);
@@ -609,7 +620,8 @@ static size_t segrows_smem() {
 template <int M>
 static size_t cols_rc_smem() {
     using G = ColsGeom<M, 128>;
-    return G::TWL * sizeof(float2) + (size_t)(2 * G::CP + 1) * G::CS * sizeof(float2) + 2 * sizeof(double);
+    return G::TWL * sizeof(float2) + (size_t)(2 * G::CP + 1) * G::CS * sizeof(float2) +
+           (size_t)(M + G::CP + 1) * sizeof(float2) + 4 * sizeof(double);
 }
 
 template <int N>
