@@ -440,14 +440,17 @@ Plan rows_subrange(Plan P, int off, int n) {
 }
 
 int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len) {
-    // As many windows per batch as the scratch holds: one 1000-window launch
-    // per stage fills the GPU better than two overlapped 500-window batches
-    // (0.758 against 0.792 ms on the 128x128 case); jobs larger than the
-    // scratch still alternate between the two slots.  The precision form is
-    // the exception: its one-CTA-per-SM tensor stages gain more from two
-    // batches overlapping on the two slots (626 K against 601 K windows/s).
+    // With one row stage per window, as many windows per batch as the scratch
+    // holds: one 1000-window launch per stage fills the GPU better than two
+    // overlapped 500-window batches (0.758 against 0.792 ms on the 128x128
+    // case); jobs larger than the scratch alternate between the two slots.
+    // Two batches for jobs of 512 windows or more on the precision form (its
+    // one-CTA-per-SM tensor stages: 626 K against 601 K windows/s) and on
+    // shared row segments (the second batch's row stage overlaps the first's
+    // column stage: 0.548 against 0.563 ms per 1000 windows of 128x128, and
+    // in the host entry its image copy too: 0.732 against 0.791 ms).
     int bw = c->max_batch;
-    if (c->base.tc_form && nlocs >= 512 && (nlocs + 1) / 2 < bw) bw = (nlocs + 1) / 2;
+    if ((c->base.tc_form || c->base.rc) && nlocs >= 512 && (nlocs + 1) / 2 < bw) bw = (nlocs + 1) / 2;
     if (strip_len > 0 && strip_len <= bw) bw = ((bw + strip_len - 1) / strip_len) * strip_len;   // whole strips
     if (bw > c->max_batch) bw = (c->max_batch / (strip_len > 0 ? strip_len : 1)) * (strip_len > 0 ? strip_len : 1);
     if (bw < 1) bw = c->max_batch;
@@ -629,6 +632,32 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
             hi = std::max(hi, std::min(y0 + npy, ny[k]));
         }
     };
+    // columns [c0, c1) of image k that any window reads: the copies move only
+    // that part of each row (the rest of the device image is never read)
+    int c0[2], c1[2];
+    {
+        const int nx[2] = {m_nx, s_nx};
+        const int npx = c->base.npx;
+        for (int k = 0; k < 2; k++) {
+            c0[k] = nx[k]; c1[k] = 0;
+            for (int w = 0; w < nlocs; w++) {
+                const int x0 = locs[w].x + (k ? x_offset : 0) - npx / 2;
+                c0[k] = std::min(c0[k], std::max(x0, 0));
+                c1[k] = std::max(c1[k], std::min(x0 + npx, nx[k]));
+            }
+            if (c1[k] <= c0[k]) { c0[k] = 0; c1[k] = 0; }      // every window outside: nothing to copy
+        }
+    }
+    // rows [r0, r1) of image k, columns [c0, c1), on the copy stream
+    auto copy_rows = [&](int k, int r0, int r1) -> xcg_status {
+        if (r1 <= r0 || c1[k] <= c0[k]) return XCG_OK;
+        const size_t off = (size_t)r0 * rowb[k] + (size_t)c0[k] * es;
+        XCG_CK(cudaMemcpy2DAsync((char *)c->d_img[k] + off, rowb[k], (const char *)src[k] + off, rowb[k],
+                                 (size_t)(c1[k] - c0[k]) * es, (size_t)(r1 - r0), cudaMemcpyHostToDevice,
+                                 c->copy_stream),
+               k ? "copy slave" : "copy master");
+        return XCG_OK;
+    };
     int done[2];
     for (int k = 0; k < 2; k++) {
         int lo, hi;
@@ -656,11 +685,8 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
                 for (int k = 0; k < 2; k++) {
                     const int end = std::min(hi[k], Qb.rc_band_end[k][b]);
                     if (end > done[k]) {
-                        XCG_CK(cudaMemcpyAsync((char *)c->d_img[k] + (size_t)done[k] * rowb[k],
-                                               (const char *)src[k] + (size_t)done[k] * rowb[k],
-                                               (size_t)(end - done[k]) * rowb[k], cudaMemcpyHostToDevice,
-                                               c->copy_stream),
-                               k ? "copy slave" : "copy master");
+                        const xcg_status cs = copy_rows(k, done[k], end);
+                        if (cs != XCG_OK) return cs;
                         done[k] = end;
                     }
                 }
@@ -686,10 +712,8 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
                 int lo, hi;
                 rows_of(Q.win0 + o0, Q.win0 + o1, k, lo, hi);
                 if (hi > done[k]) {
-                    XCG_CK(cudaMemcpyAsync((char *)c->d_img[k] + (size_t)done[k] * rowb[k],
-                                           (const char *)src[k] + (size_t)done[k] * rowb[k],
-                                           (size_t)(hi - done[k]) * rowb[k], cudaMemcpyHostToDevice, c->copy_stream),
-                           k ? "copy slave" : "copy master");
+                    const xcg_status cs = copy_rows(k, done[k], hi);
+                    if (cs != XCG_OK) return cs;
                     done[k] = hi;
                 }
             }
