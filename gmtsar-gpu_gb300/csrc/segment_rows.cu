@@ -165,17 +165,17 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
         const int c0 = rlen[r] + (key_y(key[i]) - key_y(key[rhead[r]])) / rpc;
         reinterpret_cast<int *>(P.rc_wch)[pay[i]] = c0;   // rc_wch[w].x for the master, .y for the slave
     }
-    // chunk descriptors, each chunk's run by binary search over the runs' first chunks
-    for (int c = tid; c < total; c += PLAN_THREADS) {
-        int lo = 0, hi = nruns - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (rlen[mid] <= c) lo = mid; else hi = mid - 1;
+    // chunk descriptors: one warp per run, its lanes writing consecutive chunks
+    {
+        const int wp = tid >> 5, l32 = tid & 31;
+        for (int r = wp; r < nruns; r += PLAN_THREADS / 32) {
+            const unsigned long long k = key[rhead[r]];
+            const int pidx = (int)(k >> 49), img = (int)((k >> 48) & 1);
+            const int x0 = (int)((k >> 28) & ((1u << 20) - 1)) - KEY_X_BIAS;
+            const int y0 = key_y(k);
+            const int c0 = rlen[r], c1 = (r + 1 < nruns) ? rlen[r + 1] : total;
+            for (int c = c0 + l32; c < c1; c += 32) P.rc_desc[c] = make_int4(pidx, img, x0, y0 + (c - c0) * rpc);
         }
-        const unsigned long long k = key[rhead[lo]];
-        const int pidx = (int)(k >> 49), img = (int)((k >> 48) & 1);
-        const int x0 = (int)((k >> 28) & ((1u << 20) - 1)) - KEY_X_BIAS;
-        P.rc_desc[c] = make_int4(pidx, img, x0, key_y(k) + (c - rlen[lo]) * rpc);
     }
     if (tid == 0) *P.rc_count = total;
     if (P.rc_nbands > 0) {

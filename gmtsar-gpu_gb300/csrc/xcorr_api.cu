@@ -481,6 +481,11 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     // from and joined back into s); profiling runs them in order on s so each
     // kernel's events time that kernel alone
     const bool fork = nb > 1 && c->nslots > 1 && !c->profiling;
+    for (int b = 0; b < nb; b++)           // before anything is enqueued
+        if (starts[b + 1] - starts[b] > c->max_batch) {
+            set_last_error("batch larger than the context's scratch");
+            return XCG_ERR_TOO_LARGE;
+        }
     if (tcf) {             // a timeout of an earlier call must not be reported by this one
         const xcg_status rs = tc_reset_status(c, s);
         if (rs != XCG_OK) return rs;
@@ -488,6 +493,19 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     if (fork) {
         XCG_CK(cudaEventRecord(c->ev_fork, s), "cudaEventRecord");
         for (int k = 0; k < c->nslots; k++) XCG_CK(cudaStreamWaitEvent(c->slot_stream[k], c->ev_fork, 0), "cudaStreamWaitEvent");
+    }
+    // shared row segments through the device entry: the first batches'
+    // planners (one CTA each, reading only the locations) go first on their
+    // slot streams, so a later batch's plan is ready when its rows start
+    // instead of waiting for an SM behind the earlier batch's row stage
+    const int npre = (rc && fork && !rows) ? std::min(nb, c->nslots) : 0;
+    for (int b = 0; b < npre; b++) {
+        Plan Q = with_slot(P, (size_t)b * c->slot_bytes);
+        Q.win0 = starts[b];
+        Q.nwin = starts[b + 1] - starts[b];
+        Q.locs = locs0 + Q.win0;
+        Q.winref = ref0 ? ref0 + Q.win0 : nullptr;
+        launch_rc_plan(Q, c->slot_stream[b]);
     }
     for (int b = 0; b < nb; b++) {
         const int slot = fork ? b % c->nslots : 0;
@@ -517,8 +535,13 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
             } else {
                 switch (k) {
                     case 0:
-                        if (rc) { launch_rc_plan(Q, ss); launch_segrows(Q, ss); c->stats.launches++; }
-                        else launch_rows(Q, ss);
+                        if (rc) {
+                            if (b >= npre) launch_rc_plan(Q, ss);
+                            launch_segrows(Q, ss);
+                            c->stats.launches++;
+                        } else {
+                            launch_rows(Q, ss);
+                        }
                         break;
                     case 1:
                         if (tm) launch_tcorr(Q, ss);
