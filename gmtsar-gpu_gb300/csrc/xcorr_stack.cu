@@ -97,12 +97,13 @@ static xcg_status get_bucket(xcg_stack *st, int xs, int ys, Bucket **out) {
         if (f) {
             char line[256];
             while (fgets(line, sizeof line, f)) {
-                int a, bb, r, i, bt, cc = 0, pc = 0;
-                const int n = sscanf(line, "%d %d %d %d %d %d %d", &a, &bb, &r, &i, &bt, &cc, &pc);
+                int a, bb, r, i, bt, cc = 0, pc = 0, sh = 1;
+                const int n = sscanf(line, "%d %d %d %d %d %d %d %d", &a, &bb, &r, &i, &bt, &cc, &pc, &sh);
                 if (n < 5 || a != 4 * xs || bb != 4 * ys || r != p.ri || i != p.interp_factor) continue;
                 b.batch = bt;
                 b.ctx->base.cols_cfg = (n >= 7 && cc >= 0 && cc <= 2) ? cc : 0;
                 b.ctx->base.peak_cfg = (n >= 7 && pc >= 0 && pc <= 1) ? pc : 0;
+                b.ctx->base.rc = (n >= 8 && sh == 0) ? 0 : 1;
             }
             fclose(f);
         }
@@ -262,6 +263,7 @@ void xcg_stack_get_stats(const xcg_stack *st, xcg_stack_stats *out) {
         out->bucket_batch[k] = st->buckets[k].batch > 0 ? st->buckets[k].batch : st->buckets[k].ctx->max_batch;
         out->bucket_cols_cfg[k] = st->buckets[k].ctx->base.cols_cfg;
         out->bucket_peak_cfg[k] = st->buckets[k].ctx->base.peak_cfg;
+        out->bucket_row_sharing[k] = st->buckets[k].ctx->base.rc;
     }
 }
 
@@ -311,9 +313,11 @@ xcg_status xcg_stack_run(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, v
 }
 
 // Pick each bucket's windows per batch and launch shapes by timing
-// candidates on these pairs: batch sizes first (default shapes), then the
-// column stage's shape (columns per CTA, staging depth), then the peak
-// stage's residency, each keeping the best so far.
+// candidates on these pairs: batch sizes first (shared row segments, default
+// shapes), then the row/column stages (shared row segments, or one row stage
+// per window with each of the per-window column stage's shapes: columns per
+// CTA, staging depth), then the peak stage's residency, each keeping the best
+// so far.
 xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, void *stream) {
     if (!st || npairs <= 0 || !pairs) return XCG_ERR_ARG;
     XCG_TRY(ck(cudaSetDevice(st->device), "cudaSetDevice"));
@@ -354,6 +358,7 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
         };
         B.cols_cfg = 0;
         B.peak_cfg = 0;
+        B.rc = 1;
         std::vector<int> cands;
         for (int c : {128, 256, 512, 1024, 2048, 4096})
             if (c < b.ctx->max_batch && c < nwin) cands.push_back(c);
@@ -367,14 +372,16 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
             if (t < best) { best = t; bestc = c; }
         }
         b.batch = bestc;
-        int best_cols = 0, best_peak = 0;
-        for (int cfg = 1; cfg <= 2; cfg++) {
+        int best_cols = 0, best_peak = 0, best_share = 1;
+        B.rc = 0;                                         // one row stage per window, each column shape
+        for (int cfg = 0; cfg <= 2; cfg++) {
             B.cols_cfg = cfg;
             float t;
             XCG_TRY(time_it(&t));
-            if (t < best) { best = t; best_cols = cfg; }
+            if (t < best) { best = t; best_cols = cfg; best_share = 0; }
         }
-        B.cols_cfg = best_cols;
+        B.rc = best_share;
+        B.cols_cfg = best_share ? 0 : best_cols;
         B.peak_cfg = 1;
         {
             float t;
@@ -385,8 +392,8 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
         if (cache) {
             FILE *f = fopen(cache, "a");
             if (f) {
-                fprintf(f, "%d %d %d %d %d %d %d\n", 4 * b.xs, 4 * b.ys, st->common.ri, st->common.interp_factor, bestc,
-                        best_cols, best_peak);
+                fprintf(f, "%d %d %d %d %d %d %d %d\n", 4 * b.xs, 4 * b.ys, st->common.ri, st->common.interp_factor,
+                        bestc, B.cols_cfg, best_peak, best_share);
                 fclose(f);
             }
         }

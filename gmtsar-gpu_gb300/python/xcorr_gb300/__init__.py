@@ -96,7 +96,7 @@ class StackStats(ctypes.Structure):
                 ("last_graph_batches", ctypes.c_int32), ("buckets", ctypes.c_int32), ("pad", ctypes.c_int32),
                 ("bucket_npx", ctypes.c_int32 * 8), ("bucket_npy", ctypes.c_int32 * 8),
                 ("bucket_batch", ctypes.c_int32 * 8), ("bucket_cols_cfg", ctypes.c_int32 * 8),
-                ("bucket_peak_cfg", ctypes.c_int32 * 8)]
+                ("bucket_peak_cfg", ctypes.c_int32 * 8), ("bucket_row_sharing", ctypes.c_int32 * 8)]
 
 _lib = None
 

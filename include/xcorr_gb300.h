@@ -187,6 +187,7 @@ typedef struct {
     int32_t bucket_cols_cfg[8];  /* column-stage launch shape: 0 128-thread CTAs, two cp.async staging groups;
                                     1 256-thread CTAs; 2 one staging group */
     int32_t bucket_peak_cfg[8];  /* peak-stage residency: 0 four CTAs per SM, 1 three */
+    int32_t bucket_row_sharing[8];  /* 1: shared row segments (bucket_cols_cfg unused), 0: one row stage per window */
 } xcg_stack_stats;
 
 typedef struct xcg_stack xcg_stack;
@@ -204,10 +205,11 @@ xcg_status xcg_stack_run(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, v
  * and locations replay it. */
 void xcg_stack_set_graph(xcg_stack *st, int32_t enable);
 /* Time candidates per bucket on these pairs and keep the fastest: windows per
- * batch, then the column stage's launch shape (column pairs per CTA, cp.async
- * staging depth), then the peak stage's residency (appended to the file named
- * by XCG_TUNE_CACHE as "npx npy ri interp_factor batch cols_cfg peak_cfg",
- * read back by new buckets). */
+ * batch, then the row/column stages (shared row segments, or one row stage
+ * per window with each column-stage launch shape: column pairs per CTA,
+ * cp.async staging depth), then the peak stage's residency (appended to the
+ * file named by XCG_TUNE_CACHE as "npx npy ri interp_factor batch cols_cfg
+ * peak_cfg row_sharing", read back by new buckets). */
 xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npairs, void *stream);
 void xcg_stack_get_stats(const xcg_stack *st, xcg_stack_stats *out);
 

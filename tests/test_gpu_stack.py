@@ -114,11 +114,16 @@ def test_autotune_and_split_strips(tmp_path, monkeypatch):
         it["dr"].zero_()
     st.run(_pairs(items), 0)
     torch.cuda.synchronize()
+    # the tuner may pick one row stage per window for a bucket: the same
+    # peaks and offsets, the correlation within FP32 rounding
     for it, a in zip(items, alone):
         if it["nxl"] <= 7:
-            _same(_host(it["dr"]), a)
+            got = _host(it["dr"])
+            for k in ("ip", "jp", "fip", "fjp", "flags", "xoff", "yoff", "xfrac", "yfrac"):
+                np.testing.assert_array_equal(got[k], a[k], err_msg=k)
+            assert np.max(np.abs(got["gamma"] / a["gamma"] - 1)) < 1e-5
     lines = cache.read_text().splitlines()
-    assert len(lines) >= 1 + 4 and all(len(l.split()) == 7 for l in lines[1:])
+    assert len(lines) >= 1 + 4 and all(len(l.split()) == 8 for l in lines[1:])
     s = st.stats()
     assert all(0 <= s.bucket_cols_cfg[i] <= 2 and 0 <= s.bucket_peak_cfg[i] <= 1 for i in range(s.buckets))
     st.close()
@@ -158,16 +163,22 @@ def test_stack_every_bucket_against_oracle():
     st.close()
 
 
-@pytest.mark.parametrize("cols_cfg,peak_cfg", [(1, 0), (2, 1), (1, 1)])
+@pytest.mark.parametrize("cols_cfg,peak_cfg", [(0, 1), (1, 0), (2, 1), (1, 1)])
 def test_tuned_launch_shapes_give_identical_results(tmp_path, monkeypatch, cols_cfg, peak_cfg):
-    """Every launch shape the autotuner chooses between (256-thread column
-    CTAs, one cp.async staging group, three peak CTAs per SM) computes the
-    same transforms in the same order: results bit-identical to the default."""
+    """Every per-window launch shape the autotuner chooses between (256-thread
+    column CTAs, one cp.async staging group, three peak CTAs per SM) computes
+    the same transforms in the same order: results bit-identical to a
+    context with one row stage per window."""
     torch = pytest.importorskip("torch")
     items = _setup(torch)
-    alone = [_alone(it) for it in items]
+    alone = []
+    for it in items:
+        with xg.Context(xg.params(it["xs"], it["ys"])) as ctx:
+            ctx.set_row_sharing(False)
+            alone.append(ctx.correlate(it["m"], it["s"], it["locs"], it["xo"], it["yo"], it["ast"],
+                                       strip_len=it["nxl"]))
     cache = tmp_path / "tune.txt"
-    cache.write_text("".join(f"{4 * xs} {4 * ys} 2 16 0 {cols_cfg} {peak_cfg}\n"
+    cache.write_text("".join(f"{4 * xs} {4 * ys} 2 16 0 {cols_cfg} {peak_cfg} 0\n"
                              for xs, ys in {(it["xs"], it["ys"]) for it in items}))
     monkeypatch.setenv("XCG_TUNE_CACHE", str(cache))
     st = xg.Stack(xg.params())
@@ -176,6 +187,7 @@ def test_tuned_launch_shapes_give_identical_results(tmp_path, monkeypatch, cols_
     s = st.stats()
     assert [s.bucket_cols_cfg[i] for i in range(s.buckets)] == [cols_cfg] * s.buckets
     assert [s.bucket_peak_cfg[i] for i in range(s.buckets)] == [peak_cfg] * s.buckets
+    assert [s.bucket_row_sharing[i] for i in range(s.buckets)] == [0] * s.buckets
     for it, a in zip(items, alone):
         _same(_host(it["dr"]), a)
     st.close()
