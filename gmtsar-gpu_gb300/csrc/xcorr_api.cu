@@ -679,6 +679,7 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
                                  (size_t)(c1[k] - c0[k]) * es, (size_t)(r1 - r0), cudaMemcpyHostToDevice,
                                  c->copy_stream),
                k ? "copy slave" : "copy master");
+        c->stats.h2d_bytes += (int64_t)(c1[k] - c0[k]) * (int64_t)es * (r1 - r0);
         return XCG_OK;
     };
     int done[2];
@@ -755,6 +756,8 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     };
     memset(&c->stats, 0, sizeof c->stats);
     c->stats.scratch_bytes = c->scratch_bytes;
+    c->stats.h2d_bytes = (int64_t)nlocs * (int64_t)sizeof(xcg_loc);
+    c->stats.d2h_bytes = (int64_t)nlocs * (int64_t)sizeof(xcg_result);
     xcg::Plan P = xcg::ctx_plan(c);
     P.single.master = c->d_img[0]; P.single.m_nx = m_nx; P.single.m_ny = m_ny;
     P.single.slave = c->d_img[1]; P.single.s_nx = s_nx; P.single.s_ny = s_ny;

@@ -57,7 +57,8 @@ RESULT_DTYPE = np.dtype([
 class Stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64), ("batches", ctypes.c_int32), ("batch_windows", ctypes.c_int32),
                 ("kernel_ms", ctypes.c_double * 8), ("scratch_bytes", ctypes.c_size_t),
-                ("nkernels", ctypes.c_int32), ("pad", ctypes.c_int32), ("row_chunks", ctypes.c_int64)]
+                ("nkernels", ctypes.c_int32), ("pad", ctypes.c_int32), ("row_chunks", ctypes.c_int64),
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
 
 
 KERNEL_NAMES = ("k_rows", "k_cols", "k_peak", "k_subpix")

@@ -93,6 +93,9 @@ typedef struct {
     int32_t pad;
     int64_t row_chunks;        /* with profiling and shared row segments: 1024-sample chunks the row stage
                                   computed (2 x nchunks per window without sharing) */
+    int64_t h2d_bytes;         /* xcg_correlate: bytes copied host to device (the image rows and columns
+                                  the windows read, the locations); 0 for the device entries */
+    int64_t d2h_bytes;         /* xcg_correlate: bytes copied device to host (the result records) */
 } xcg_stats;
 
 const char *xcg_status_string(xcg_status s);

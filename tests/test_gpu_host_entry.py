@@ -44,8 +44,17 @@ def test_sub_area_and_stale_buffers(pairs):
     with xg.Context(xg.params(64, 64), max_batch=96) as ctx:
         ctx.correlate(m1, s1, full, strip_len=6)                  # fills the image buffers with pair 1
         r = ctx.correlate(m2, s2, part, strip_len=6)              # reads only pair 2's rows it copies
+        st = ctx.stats()
         d = _device(ctx, m2, s2, part, 6)
     _same(r, d)
+    # the bytes it reports copying: the rows and columns of both images that
+    # the 256 x 256 patches cover (no offsets here), the locations, the results
+    y0, x0 = part[:, 1] - 128, part[:, 0] - 128
+    rows = min(int(y0.max()) + 256, 3072) - max(int(y0.min()), 0)
+    cols = min(int(x0.max()) + 256, 1024) - max(int(x0.min()), 0)
+    assert st.h2d_bytes == 2 * rows * cols * 4 + part.nbytes
+    assert st.h2d_bytes < m2.nbytes
+    assert st.d2h_bytes == len(part) * xg.RESULT_DTYPE.itemsize
 
 
 def test_location_order_and_shifted_slave(pairs):
