@@ -28,8 +28,12 @@
 //   k_cols_rc   per group of columns kx of one window: the column FFTs of
 //               the master's and the masked slave's half spectra, the
 //               product with the demean/mask corrections and the inverse
-//               column FFT of the surface rows, as k_cols
+//               column FFT of the surface rows, as k_cols; the default form
+//               (k_cols_rcp) is persistent, each CTA walking a range of
+//               (window, column group) tiles with the next tile's rows staged
+//               while the current one is transformed
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <math.h>
 #include <stdint.h>
 
@@ -179,30 +183,54 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
     }
     if (tid == 0) *P.rc_count = total;
     if (P.rc_nbands > 0) {
-        // counting sort of the chunks by row band (order within a band is free)
+        // the chunks listed band by band (order within a band is free).  A
+        // chunk belongs to the first band whose end row lies beyond its last
+        // row (the last band takes the rest).  Chunk k of a run covers rows
+        // y0 + k rpc .. y0 + k rpc + rpc - 1, increasing with k, so each band's
+        // chunks are one range of the run, found from the band ends alone:
+        // one warp per run counts them, then writes its ranges at offsets
+        // taken from per-band counters
         int *bcnt = wsum;                         // [0, 8) counts, [8, 16) fill, [16, 24) starts
         const int nb = P.rc_nbands;
-        __syncthreads();                          // descriptors written; wsum free
-        if (tid < 32) wsum[tid] = 0;
+        const int wp = tid >> 5, l32 = tid & 31;
+        __syncthreads();                          // wsum free (the scans are done)
+        if (tid < 24) wsum[tid] = 0;
         __syncthreads();
-        auto band_of = [&](int c) {
-            const int4 d = P.rc_desc[c];
-            const int last = d.w + rpc - 1;
-            int b = 0;
-            while (b < nb - 1 && last >= P.rc_band_end[d.y][b]) b++;
-            return b;
+        // chunks of a run (first row y0, len chunks) whose last row is below row e
+        auto below = [&](long long e, int y0, int len) {
+            const long long num = e - (long long)y0 - rpc + 1;     // k rpc < num
+            const long long k = (num <= 0) ? 0 : (num + rpc - 1) / rpc;
+            return (int)(k < len ? k : len);
         };
-        for (int c = tid; c < total; c += PLAN_THREADS) atomicAdd(&bcnt[band_of(c)], 1);
-        __syncthreads();
-        if (tid == 0) {
-            int acc = 0;
-            for (int b = 0; b < nb; b++) { bcnt[16 + b] = acc; P.rc_band_start[b] = acc; acc += bcnt[b]; }
-            P.rc_band_start[nb] = acc;
-        }
-        __syncthreads();
-        for (int c = tid; c < total; c += PLAN_THREADS) {
-            const int b = band_of(c);
-            P.rc_order[bcnt[16 + b] + atomicAdd(&bcnt[8 + b], 1)] = c;
+        for (int pass = 0; pass < 2; pass++) {
+            for (int r = wp; r < nruns; r += PLAN_THREADS / 32) {
+                const unsigned long long k = key[rhead[r]];
+                const int img = (int)((k >> 48) & 1), y0 = key_y(k);
+                const int c0 = rlen[r], len = ((r + 1 < nruns) ? rlen[r + 1] : total) - c0;
+                int lo = 0, n = 0;                // lane b < nb: band b's chunks c0 + [lo, lo + n)
+                if (l32 < nb) {
+                    lo = (l32 == 0) ? 0 : below(P.rc_band_end[img][l32 - 1], y0, len);
+                    n = ((l32 == nb - 1) ? len : below(P.rc_band_end[img][l32], y0, len)) - lo;
+                }
+                if (pass == 0) {
+                    if (n > 0) atomicAdd(&bcnt[l32], n);
+                } else {
+                    const int off = (n > 0) ? bcnt[16 + l32] + atomicAdd(&bcnt[8 + l32], n) : 0;
+                    for (int b = 0; b < nb; b++) {
+                        const int ob = __shfl_sync(0xffffffffu, off, b);
+                        const int lb = __shfl_sync(0xffffffffu, lo, b);
+                        const int nn = __shfl_sync(0xffffffffu, n, b);
+                        for (int j = l32; j < nn; j += 32) P.rc_order[ob + j] = c0 + lb + j;
+                    }
+                }
+            }
+            __syncthreads();
+            if (pass == 0 && tid == 0) {
+                int acc = 0;
+                for (int b = 0; b < nb; b++) { bcnt[16 + b] = acc; P.rc_band_start[b] = acc; acc += bcnt[b]; }
+                P.rc_band_start[nb] = acc;
+            }
+            __syncthreads();
         }
     }
 }
@@ -603,6 +631,209 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan 
     }
 }
 
+// The column stage as a persistent, software-pipelined kernel (the default;
+// k_cols_rc above is one CTA per tile).  A tile is (window, group of CP
+// columns); each CTA takes a contiguous range of tiles, so consecutive tiles
+// are the next column groups of the same window: the twiddles and the row
+// mask's spectrum are staged once per CTA and the patch means once per
+// window.  Per tile: the slave's mask rows (staged during the previous
+// tile's inverse transform) are transformed first, then the master's
+// (staged during the previous tile's copy-out and the slave transform); the
+// master's spectrum stays in registers for the product, after which the
+// slave slots are free and the next tile's slave rows are requested.  Rows
+// outside the slave's mask are zero in registers, never staged.  The
+// arithmetic is k_cols_rc's, operation for operation, so the results are the
+// same bits.  Tiles of column group 0 (the packed DC/Nyquist column, whose
+// second output goes through the slave slot) take k_cols_rc's order.
+template <int M, int THR>
+__global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan P) {
+    using G = ColsGeom<M, THR>;
+    constexpr int T = G::T, CS = G::CS, CP = G::CP, TWL = G::TWL;
+    constexpr int PER = M / T;
+    constexpr int RSTEP = THR / CP;            // rows a staging pass covers
+    static_assert((CP & (CP - 1)) == 0 && T % 2 == 0, "columns per CTA: a power of two");
+    static_assert(THR == 128, "four warps: two partial chunk sums per patch");
+    static_assert(PER % 4 == 0 && (M / 2) % RSTEP == 0, "mask rows: whole registers and staging passes");
+
+    extern __shared__ float4 smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *cols = tw + TWL;                   // [2*CP + 1][CS]: master, slave, kx = N/2 product
+    float2 *boxy = cols + (2 * CP + 1) * CS;    // [M] DFT of the row mask
+    float2 *boxx = boxy + M;                    // [CP + 1] DFT of the column mask at this tile's kx, then N/2
+    double *dsum = reinterpret_cast<double *>(boxx + CP + 1);   // [4] per-warp partial chunk sums
+
+    const int N = P.npx, NH = N / 2;
+    const int NG = NH / CP;                     // column groups per window
+    const int ntiles = P.nwin * NG;
+    const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+    const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+    if (t0 >= t1) return;
+    const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
+    const int lane = l32 % T;
+    const int team = warp * (32 / T) + l32 / T;
+    const int sl = threadIdx.x % CP, row0 = threadIdx.x / CP;   // staging: slot, first row
+
+    // tile t's slave mask rows [M/4, 3M/4) / master rows, into the slots (one commit group each)
+    auto stage_slave = [&](int t) {
+        const int w = t / NG, kx0 = (t - w * NG) * CP;
+        const float2 *src = P.rc_spec + (size_t)P.rc_wch[w].y * P.rpc * NH + kx0 + sl;
+        float2 *slot = cols + (CP + sl) * CS;
+#pragma unroll 8
+        for (int k = 0; k < (M / 2) / RSTEP; k++) {
+            const int r = M / 4 + row0 + k * RSTEP;
+            cp_async8(slot + fft_pad(r), src + (size_t)r * NH);
+        }
+        cp_async_commit();
+    };
+    auto stage_master = [&](int t) {
+        const int w = t / NG, kx0 = (t - w * NG) * CP;
+        const float2 *src = P.rc_spec + (size_t)P.rc_wch[w].x * P.rpc * NH + kx0 + sl;
+        float2 *slot = cols + sl * CS;
+#pragma unroll 8
+        for (int k = 0; k < M / RSTEP; k++) {
+            const int r = row0 + k * RSTEP;
+            cp_async8(slot + fft_pad(r), src + (size_t)r * NH);
+        }
+        cp_async_commit();
+    };
+
+    stage_slave(t0);
+    stage_master(t0);
+    for (int i = threadIdx.x; i < TWL; i += THR) tw[i] = P.tw_col[i];
+    for (int i = threadIdx.x; i < M; i += THR) boxy[i] = __ldg(P.box_y + i);
+
+    int cur_w = -1;
+    float dc1 = 0.f, m2 = 0.f;
+    for (int t = t0; t < t1; t++) {
+        const int w = t / NG, b = t - w * NG, kx0 = b * CP;
+        const bool neww = (w != cur_w);
+        // (the previous tile's last barrier ordered every read of boxx and dsum before these writes)
+        if (threadIdx.x <= CP) boxx[threadIdx.x] = __ldg(P.box_x + (threadIdx.x < CP ? kx0 + threadIdx.x : NH));
+        if (neww) {
+            // patch means from the chunk sums (conv_ampl_demean.cu:719-724),
+            // warps 0-1 the master's, 2-3 the slave's (exact in double: any order)
+            const int2 wc = P.rc_wch[w];
+            const int base = (warp < 2) ? wc.x : wc.y;
+            double sp = 0.0;
+            for (int i = (warp & 1) * 32 + l32; i < P.nchunks; i += 64) sp += (double)P.rc_part[base + i];
+            sp = warp_sum_f64(sp);
+            if (l32 == 0) dsum[warp] = sp;
+        }
+        cp_async_wait<1>();                      // this tile's slave rows in (this thread's copies)
+        __syncthreads();                         // ... and everyone's; boxx, dsum, tw, boxy written
+        if (neww) {
+            const double inv = pow2_inv(N * M);
+            const double s1 = (dsum[0] + dsum[1]) * inv, s2 = (dsum[2] + dsum[3]) * inv;
+            dc1 = (float)(s1 * (double)N * (double)M);
+            m2 = (float)s2;
+            if (b == 0 && threadIdx.x == 0) { P.means[2 * w] = s1; P.means[2 * w + 1] = s2; }
+            cur_w = w;
+        }
+
+        const int kx = kx0 + team;
+        float2 *a = cols + team * CS;            // master column, later the result
+        float2 *pa = cols + (CP + team) * CS;    // slave column
+        float2 z[PER];
+#pragma unroll
+        for (int m = 0; m < PER; m++)
+            z[m] = (m >= PER / 4 && m < 3 * PER / 4) ? pa[fft_pad(lane + T * m)] : make_float2(0.f, 0.f);
+        __syncwarp();
+        team_fft_reg<M, -1>(z, pa, tw, lane);
+#pragma unroll
+        for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
+        cp_async_wait<0>();                      // master rows in
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < PER; m++) z[m] = a[fft_pad(lane + T * m)];
+        __syncwarp();
+        team_fft_reg<M, -1>(z, a, tw, lane);
+
+        auto product = [&](int kxx, float2 A1, float2 A2, int ky) {
+            if (kxx == 0 && ky == 0) A1.x -= dc1;
+            const float2 bm = cmulf(boxx[kxx == NH ? CP : kxx - kx0], boxy[ky]);
+            A2.x -= m2 * bm.x;
+            A2.y -= m2 * bm.y;
+            float2 pr = cmulf_conj(A1, A2);
+            if ((kxx + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
+            return pr;
+        };
+        if (b != 0) {
+            // no packed column in this tile (CTA-uniform): the product from the
+            // master spectrum in registers, then the slave slots are free
+#pragma unroll
+            for (int m = 0; m < PER; m++) {
+                const int ky = lane + T * m;
+                z[m] = product(kx, z[m], pa[fft_pad(ky)], ky);
+            }
+            __syncthreads();                     // every team has read its slave column
+            if (t + 1 < t1) stage_slave(t + 1);
+            team_fft_reg<M, +1>(z, a, tw, lane);
+#pragma unroll
+            for (int m = PER / 4; m < 3 * PER / 4; m++) a[fft_pad(lane + T * m)] = z[m];
+        } else {
+            // column group 0: k_cols_rc's order, the kx = 0 team's second
+            // output (column N/2) through the extra slot into its slave slot
+#pragma unroll
+            for (int m = 0; m < PER; m++) a[fft_pad(lane + T * m)] = z[m];
+            __syncwarp();
+            const bool dc = (kx == 0);
+            const int nout = __any_sync(0xffffffffu, dc) ? 2 : 1;
+            float2 *xs = cols + 2 * CP * CS;
+#pragma unroll 1
+            for (int o = 0; o < nout; o++) {
+                if (o == 0) {
+#pragma unroll
+                    for (int m = 0; m < PER; m++) {
+                        const int ky = lane + T * m;
+                        const float2 zm = a[fft_pad(ky)], zs = pa[fft_pad(ky)];
+                        if (!dc) {
+                            z[m] = product(kx, zm, zs, ky);
+                        } else {
+                            const int kyn = (M - ky) & (M - 1);
+                            const float2 wm = a[fft_pad(kyn)], ws = pa[fft_pad(kyn)];
+                            const float2 D1 = make_float2(0.5f * (zm.x + wm.x), 0.5f * (zm.y - wm.y));
+                            const float2 D2 = make_float2(0.5f * (zs.x + ws.x), 0.5f * (zs.y - ws.y));
+                            const float2 Q1 = make_float2(0.5f * (zm.y + wm.y), -0.5f * (zm.x - wm.x));
+                            const float2 Q2 = make_float2(0.5f * (zs.y + ws.y), -0.5f * (zs.x - ws.x));
+                            z[m] = product(0, D1, D2, ky);
+                            xs[fft_pad(ky)] = product(NH, Q1, Q2, ky);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int m = 0; m < PER; m++) z[m] = xs[fft_pad(lane + T * m)];
+                }
+                float2 *dst = (o == 0) ? a : pa;
+                __syncwarp();
+                team_fft_reg<M, +1>(z, dst, tw, lane);
+#pragma unroll
+                for (int m = PER / 4; m < 3 * PER / 4; m++) dst[fft_pad(lane + T * m)] = z[m];
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        {   // rows y in [ysearch, ysearch + nyc) of the half spectrum, kx <= N/2
+            constexpr int RS = THR / CP;
+            float2 *qw = P.qspec + (size_t)w * P.nyc * P.qpitch;
+            float2 *dstq = qw + (size_t)row0 * P.qpitch + kx0 + sl;
+            const float2 *srcc = cols + sl * CS;
+            for (int k = 0; k < (M / 2) / RS; k++) {
+                const int sy = (RS % 16 == 0) ? fft_pad(row0 + M / 4) + k * (RS + RS / 16)
+                                              : fft_pad(row0 + M / 4 + k * RS);
+                dstq[(size_t)k * RS * P.qpitch] = srcc[sy];
+            }
+            if (b == 0)
+                for (int yq = threadIdx.x; yq < M / 2; yq += THR)
+                    qw[(size_t)yq * P.qpitch + NH] = cols[CP * CS + fft_pad(yq + M / 4)];
+        }
+        __syncthreads();                         // the slots are read: the next tile's rows may land
+        if (t + 1 < t1) {
+            if (b == 0) stage_slave(t + 1);
+            stage_master(t + 1);
+        }
+    }
+}
+
 // ------------------------------------------------------------------ launchers
 
 static size_t rc_plan_smem_bytes() {
@@ -635,7 +866,10 @@ static cudaError_t setup_segrows_t() {
 }
 template <int M>
 static cudaError_t setup_cols_rc_t() {
-    return cudaFuncSetAttribute(k_cols_rc<M, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_rc_smem<M>());
+    cudaError_t e = cudaFuncSetAttribute(k_cols_rc<M, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)cols_rc_smem<M>());
+    if (e) return e;
+    return cudaFuncSetAttribute(k_cols_rcp<M, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_rc_smem<M>());
 }
 
 cudaError_t segrows_setup(const Plan &P) {
@@ -701,9 +935,19 @@ void launch_segrows(const Plan &P, cudaStream_t s) {
 
 template <int M>
 static void launch_cols_rc_t(const Plan &P, cudaStream_t s) {
-    constexpr int CP = ColsGeom<M, 128>::CP;
-    dim3 grid((P.npx / 2) / CP, P.nwin);
-    k_cols_rc<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
+    using G = ColsGeom<M, 128>;
+    const int ntiles = ((P.npx / 2) / G::CP) * P.nwin;
+    if (P.cols_cfg == 1) {                       // one CTA per tile
+        dim3 grid((P.npx / 2) / G::CP, P.nwin);
+        k_cols_rc<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
+        return;
+    }
+    // persistent: one CTA per resident slot, tiles split into contiguous ranges
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = std::min(ntiles, sms * G::BLOCKS);
+    k_cols_rcp<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
 }
 void launch_cols_rc(const Plan &P, cudaStream_t s) {
     switch (P.npy) {

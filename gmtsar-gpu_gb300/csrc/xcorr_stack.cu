@@ -373,6 +373,12 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
         }
         b.batch = bestc;
         int best_cols = 0, best_peak = 0, best_share = 1;
+        B.cols_cfg = 1;                                   // shared rows, one column-stage CTA per tile
+        {
+            float t;
+            XCG_TRY(time_it(&t));
+            if (t < best) { best = t; best_cols = 1; }
+        }
         B.rc = 0;                                         // one row stage per window, each column shape
         for (int cfg = 0; cfg <= 2; cfg++) {
             B.cols_cfg = cfg;
@@ -381,7 +387,7 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
             if (t < best) { best = t; best_cols = cfg; best_share = 0; }
         }
         B.rc = best_share;
-        B.cols_cfg = best_share ? 0 : best_cols;
+        B.cols_cfg = best_cols;
         B.peak_cfg = 1;
         {
             float t;

@@ -187,10 +187,11 @@ typedef struct {
     int64_t windows, launches, graph_replays, last_graph_launches;
     int32_t batches, last_graph_batches, buckets, pad;
     int32_t bucket_npx[8], bucket_npy[8], bucket_batch[8];
-    int32_t bucket_cols_cfg[8];  /* column-stage launch shape: 0 128-thread CTAs, two cp.async staging groups;
-                                    1 256-thread CTAs; 2 one staging group */
+    int32_t bucket_cols_cfg[8];  /* column-stage launch shape (xcg_set_launch_shapes): with shared rows 0
+                                    persistent, 1 one CTA per tile; without, 0 128-thread CTAs, two cp.async
+                                    staging groups, 1 256-thread CTAs, 2 one staging group */
     int32_t bucket_peak_cfg[8];  /* peak-stage residency: 0 four CTAs per SM, 1 three */
-    int32_t bucket_row_sharing[8];  /* 1: shared row segments (bucket_cols_cfg unused), 0: one row stage per window */
+    int32_t bucket_row_sharing[8];  /* 1: shared row segments, 0: one row stage per window */
 } xcg_stack_stats;
 
 typedef struct xcg_stack xcg_stack;
@@ -226,6 +227,15 @@ void xcg_stack_get_stats(const xcg_stack *st, xcg_stack_stats *out);
  * way; the spectra differ by FP32 rounding.  The precision form and the
  * -time/-time4 modes always run the per-window row stage. */
 xcg_status xcg_set_row_sharing(xcg_ctx *ctx, int32_t enable);
+
+/* Launch shapes of this context's column and peak stages (the choices
+ * xcg_stack_autotune makes per bucket).  cols_cfg with shared row segments:
+ * 0 (default) persistent CTAs walking ranges of (window, column group)
+ * tiles, the next tile's rows staged during the current one; 1 one CTA per
+ * tile.  Without sharing: 0 128-thread CTAs, two cp.async staging groups;
+ * 1 256-thread CTAs; 2 one staging group.  peak_cfg: 0 four CTAs per SM,
+ * 1 three.  Every shape gives the same bits. */
+xcg_status xcg_set_launch_shapes(xcg_ctx *ctx, int32_t cols_cfg, int32_t peak_cfg);
 
 /* Make later xcg_correlate_device calls on this context also write, per
  * window, the 9x9 neighbourhood of the integer peak normalised by the surface

@@ -87,3 +87,20 @@ def test_device_entry_batches_and_streams():
             assert ctx.stats().batches == 4
             outs.append(np.frombuffer(out.cpu().numpy().tobytes(), dtype=xg.RESULT_DTYPE))
     _check(outs[0], outs[1], xg.params(64, 64), m, s, locs)
+
+
+@pytest.mark.parametrize("xs,ys", [(64, 64), (16, 16), (32, 128), (128, 32), (256, 64), (16, 256)])
+def test_column_stage_forms_give_the_same_bits(xs, ys):
+    """The persistent column stage (each CTA a range of (window, column
+    group) tiles, the next tile's rows staged during the current one) and
+    one CTA per tile do the same arithmetic: every result field identical,
+    also where a CTA's range starts or ends inside a window."""
+    nx, ny = max(1024, 10 * xs), max(1536, 14 * ys)
+    m, s = synth.make_pair(synth.PairSpec(nx=nx, ny=ny, dx=0.8, dy=-1.3, noise_frac=0.1, seed=3 * xs + ys))
+    locs = xg.grid(nx, ny, 7, 11, xs, ys)
+    p = xg.params(xs, ys)
+    with xg.Context(p) as ctx:
+        persistent = ctx.correlate(m, s, locs, 3, -4, 1e-3, strip_len=7)
+        ctx.set_launch_shapes(1)
+        per_tile = ctx.correlate(m, s, locs, 3, -4, 1e-3, strip_len=7)
+    assert persistent.tobytes() == per_tile.tobytes()
