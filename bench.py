@@ -612,6 +612,7 @@ def run_ours(args):
     # per-kernel times for the roofline (library events on the same stream)
     ctx.set_profiling(True)
     kms = [0.0] * 4
+    plan_ms = 0.0                       # the row-segment planners alone (a part of the row-stage slot)
     batches = 1
     row_chunks = 0
     for _ in range(max(3, min(args.steps, 20))):
@@ -622,6 +623,7 @@ def run_ours(args):
         row_chunks += st.row_chunks
         for k in range(4):
             kms[k] += st.kernel_ms[k]
+        plan_ms += st.kernel_ms[7]
     ctx.set_profiling(False)
     nprof = max(3, min(args.steps, 20))
     row_chunks /= nprof                 # 1024-sample chunks the row stage computed per step (0: per-window rows)
@@ -754,7 +756,8 @@ def run_ours(args):
                 "hbm": {"achieved": (traffic / (avg_ms / 1e3) / 1e9) if traffic else None, "peak": hbm_peak,
                         "unit": "GB/s", "frac": ((traffic / (avg_ms / 1e3) / 1e9) / hbm_peak) if traffic else None,
                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6800"},
-                "kernel_ms_per_step": {n: kms[i] / nprof for i, n in enumerate(names)}}
+                "kernel_ms_per_step": {n: kms[i] / nprof for i, n in enumerate(names)},
+                "planner_ms_per_step": plan_ms / nprof}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

@@ -474,7 +474,7 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     const bool rc = P.rc != 0;
     const int nk = (tcf ? 6 : 4) - (P.interp_flag ? 0 : 1);
     if (c->profiling) {
-        const size_t need = (size_t)nb * nk * 2;
+        const size_t need = (size_t)nb * nk * 2 + (size_t)nb * 2;   // + the planners' own pair
         while (c->events.size() < need) {
             cudaEvent_t ev;
             XCG_CK(cudaEventCreate(&ev), "cudaEventCreate");
@@ -484,6 +484,7 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     const xcg_loc *locs0 = P.locs;
     const int2 *ref0 = P.winref;
     int ei = 0, maxw = 0;
+    int pe = nb * nk * 2;                  // profiling: the planner launches' events follow the slots'
     // batches alternate between the scratch slots on the slot streams (forked
     // from and joined back into s); profiling runs them in order on s so each
     // kernel's events time that kernel alone
@@ -543,7 +544,12 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
                 switch (k) {
                     case 0:
                         if (rc) {
-                            if (b >= npre) launch_rc_plan(Q, ss);
+                            if (b >= npre) {
+                                if (c->profiling) cudaEventRecord(c->events[pe], ss);
+                                launch_rc_plan(Q, ss);
+                                if (c->profiling) cudaEventRecord(c->events[pe + 1], ss);
+                                pe += 2;
+                            }
                             launch_segrows(Q, ss);
                             c->stats.launches++;
                         } else {
@@ -590,6 +596,11 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
                 c->stats.kernel_ms[k] += ms;
                 ei += 2;
             }
+        for (; ei < pe; ei += 2) {         // the planners, a part of slot 0, also on their own
+            float ms = 0.f;
+            XCG_CK(cudaEventElapsedTime(&ms, c->events[ei], c->events[ei + 1]), "cudaEventElapsedTime");
+            c->stats.kernel_ms[7] += ms;
+        }
     }
     return XCG_OK;
 }

@@ -87,7 +87,8 @@ typedef struct {
     double kernel_ms[8];       /* per launch slot, summed CUDA-event time when profiling: rows, columns,
                                   peak, subpixel (frequency domain); rows, surface, peak, subpixel (-time);
                                   rows, row DFT, column DFT, product + inverse column DFT, peak, subpixel
-                                  (tensor-core precision form) */
+                                  (tensor-core precision form); with shared row segments slot 0 holds
+                                  the planner and the rows, and slot 7 the planner alone (device entry) */
     size_t scratch_bytes;      /* device scratch held by the context */
     int32_t nkernels;          /* launch slots used in kernel_ms */
     int32_t pad;
