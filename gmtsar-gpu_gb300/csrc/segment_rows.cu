@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan 
 #pragma unroll
     for (int m = 0; m < PER; m++) z[m] = pa[fft_pad(lane + T * m)];
     __syncwarp();
-    team_fft_reg<M, -1>(z, pa, tw, lane);
+    team_fft_reg_mid<M, -1>(z, pa, tw, lane);    // zero outside the mask rows
 #pragma unroll
     for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
     cp_async_wait<0>();                          // master columns in
@@ -672,10 +672,17 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
     const int lane = l32 % T;
     const int team = warp * (32 / T) + l32 / T;
     const int sl = threadIdx.x % CP, row0 = threadIdx.x / CP;   // staging: slot, first row
+    // tile t: window t / NG, column group t % NG (a CTA's consecutive tiles
+    // are the next column groups of one window; taking the next windows at
+    // one column group instead, so that windows sharing row chunks read them
+    // at about the same time, was 29% slower: the means on every tile)
+    auto tile = [&](int t, int &w, int &b) { w = t / NG; b = t - w * NG; };
 
     // tile t's slave mask rows [M/4, 3M/4) / master rows, into the slots (one commit group each)
     auto stage_slave = [&](int t) {
-        const int w = t / NG, kx0 = (t - w * NG) * CP;
+        int w, b;
+        tile(t, w, b);
+        const int kx0 = b * CP;
         const float2 *src = P.rc_spec + (size_t)P.rc_wch[w].y * P.rpc * NH + kx0 + sl;
         float2 *slot = cols + (CP + sl) * CS;
 #pragma unroll 8
@@ -686,7 +693,9 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
         cp_async_commit();
     };
     auto stage_master = [&](int t) {
-        const int w = t / NG, kx0 = (t - w * NG) * CP;
+        int w, b;
+        tile(t, w, b);
+        const int kx0 = b * CP;
         const float2 *src = P.rc_spec + (size_t)P.rc_wch[w].x * P.rpc * NH + kx0 + sl;
         float2 *slot = cols + sl * CS;
 #pragma unroll 8
@@ -705,7 +714,9 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
     int cur_w = -1;
     float dc1 = 0.f, m2 = 0.f;
     for (int t = t0; t < t1; t++) {
-        const int w = t / NG, b = t - w * NG, kx0 = b * CP;
+        int w, b;
+        tile(t, w, b);
+        const int kx0 = b * CP;
         const bool neww = (w != cur_w);
         // (the previous tile's last barrier ordered every read of boxx and dsum before these writes)
         if (threadIdx.x <= CP) boxx[threadIdx.x] = __ldg(P.box_x + (threadIdx.x < CP ? kx0 + threadIdx.x : NH));
@@ -738,7 +749,7 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
         for (int m = 0; m < PER; m++)
             z[m] = (m >= PER / 4 && m < 3 * PER / 4) ? pa[fft_pad(lane + T * m)] : make_float2(0.f, 0.f);
         __syncwarp();
-        team_fft_reg<M, -1>(z, pa, tw, lane);
+        team_fft_reg_mid<M, -1>(z, pa, tw, lane);    // zero outside the mask rows
 #pragma unroll
         for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
         cp_async_wait<0>();                      // master rows in
@@ -942,11 +953,13 @@ static void launch_cols_rc_t(const Plan &P, cudaStream_t s) {
         k_cols_rc<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
         return;
     }
-    // persistent: one CTA per resident slot, tiles split into contiguous ranges
+    // persistent: one CTA per resident slot (cols_cfg 2: one slot per SM left
+    // to the other scratch slot's kernels), tiles split into contiguous ranges
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int grid = std::min(ntiles, sms * G::BLOCKS);
+    const int per_sm = (P.cols_cfg == 2 && G::BLOCKS > 1) ? G::BLOCKS - 1 : G::BLOCKS;
+    const int grid = std::min(ntiles, sms * per_sm);
     k_cols_rcp<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
 }
 void launch_cols_rc(const Plan &P, cudaStream_t s) {

@@ -165,6 +165,29 @@ __device__ __forceinline__ void dft_reg(float2 *v) {
     for (int i = 0; i < R; i++) v[i] = t[i];
 }
 
+// 16-point DFT of a sequence that is zero outside elements [4, 12), natural
+// order in and out: the first butterfly level pairs element k with k + 8,
+// one of which is zero, so that level is copies and negations.
+template <int DIR>
+__device__ __forceinline__ void dft16_mid(float2 *v) {
+    float2 t[16];
+#pragma unroll
+    for (int i = 0; i < 16; i += 2) {
+        const int k = bitrev_c<16>(i);           // 0..7
+        if (k < 4) {                              // element k is zero
+            const float2 b = v[k + 8];
+            t[i] = b;
+            t[i + 1] = make_float2(-b.x, -b.y);
+        } else {                                  // element k + 8 is zero
+            t[i] = v[k];
+            t[i + 1] = v[k];
+        }
+    }
+    dft_level<16, 4, DIR>(t);
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = t[i];
+}
+
 // One Stockham pass.  tw: this pass's twiddles [R-1][Ns] (forward sign).
 template <int N, int R, int DIR>
 __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
@@ -245,7 +268,10 @@ __host__ __device__ constexpr float sin32(int k) { return cos32(k - 8); }
 // A(lane) = exp(i pi lane / N) rides on the next pass's twiddles (the pass-0
 // outputs of lane l are the next pass's inputs r = l), whose table must then
 // hold exp(-2 pi i r (k + 1/2) / N) (half_shift_twiddles).
-template <int N, int DIR, int PASS, bool HS = false>
+// ZMID: the sequence is zero outside registers [N/T/4, 3N/T/4), i.e. outside
+// elements [N/4, 3N/4) (a masked column); the first pass then skips the
+// butterflies with a zero input (its 16-point DFTs see elements [4, 12) only).
+template <int N, int DIR, int PASS, bool HS = false, bool ZMID = false>
 __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const float2 *tw, int Ns, int lane) {
     constexpr int T = fft_lanes(N);
     constexpr int NP = fft_npasses(N);
@@ -254,6 +280,7 @@ __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const f
     constexpr int IT = NR / T;                 // butterflies per lane in this pass
     static_assert(IT * R * T == N, "team layout");
     static_assert(!HS || (DIR > 0 && N / T == 16 && IT == 1 && NP == 2), "half-sample shift: N = 128 or 256");
+    static_assert(!ZMID || (fft_radix(N, 0) == 16 && !HS), "zero outside the middle half: radix-16 first pass");
     if constexpr (PASS == 0) {
         // inputs from registers: element (lane + T*it) + NR*r = lane + T*(it + r*IT)
 #pragma unroll
@@ -269,7 +296,8 @@ __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const f
                     u[r] = make_float2(u[r].x * c - u[r].y * s, u[r].x * s + u[r].y * c);
                 }
             }
-            dft_reg<R, DIR>(u);
+            if constexpr (ZMID) dft16_mid<DIR>(u);
+            else dft_reg<R, DIR>(u);
             const int j = lane + T * it;
 #pragma unroll
             for (int r = 0; r < R; r++) ex[fft_pad(j * R + r)] = u[r];
@@ -320,6 +348,12 @@ __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const f
 template <int N, int DIR>
 __device__ __forceinline__ void team_fft_reg(float2 *v, float2 *ex, const float2 *tw, int lane) {
     team_fft_reg_pass<N, DIR, 0>(v, ex, tw, 1, lane);
+}
+
+// The same for a sequence that is zero outside elements [N/4, 3N/4).
+template <int N, int DIR>
+__device__ __forceinline__ void team_fft_reg_mid(float2 *v, float2 *ex, const float2 *tw, int lane) {
+    team_fft_reg_pass<N, DIR, 0, false, true>(v, ex, tw, 1, lane);
 }
 
 // Inverse FFT of X[f] * exp(i pi f' / N) / N (the odd samples of a 2x

@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <chrono>
 #include <complex>
 #include <functional>
 #include <string>
@@ -47,6 +48,12 @@ xcg_status cuda_fail(cudaError_t e, const char *what) {
     do {                                                     \
         cudaError_t e_ = (call);                             \
         if (e_ != cudaSuccess) return cuda_fail(e_, what);   \
+    } while (0)
+
+#define XCG_TRY_ST(expr)                       \
+    do {                                       \
+        const xcg_status st_ = (expr);         \
+        if (st_ != XCG_OK) return st_;         \
     } while (0)
 
 bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
@@ -326,6 +333,7 @@ void xcg_destroy(xcg_ctx *c) {
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->copy_stream) { cudaStreamSynchronize(c->copy_stream); cudaStreamDestroy(c->copy_stream); }
     for (cudaEvent_t ev : c->band_ready) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : c->tl_events) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -348,7 +356,7 @@ void xcg_set_features(xcg_ctx *c, float *d_features) {
 }
 
 void xcg_set_profiling(xcg_ctx *c, int32_t enable) {
-    if (c) c->profiling = enable ? 1 : 0;
+    if (c) c->profiling = (enable == 2) ? 2 : (enable ? 1 : 0);
 }
 
 void xcg_get_stats(const xcg_ctx *c, xcg_stats *out) {
@@ -381,7 +389,11 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
     std::vector<int> starts;
     for (int w = 0; w < nlocs; w += bw) starts.push_back(w);
     starts.push_back(nlocs);
-    return xcg::ctx_launch(c, P, starts.data(), (int)starts.size() - 1, (cudaStream_t)stream);
+    c->tl_tags.clear();
+    if (c->profiling == 2) XCG_TRY_ST(xcg::tl_mark(c, (cudaStream_t)stream, 1));
+    XCG_TRY_ST(xcg::ctx_launch(c, P, starts.data(), (int)starts.size() - 1, (cudaStream_t)stream));
+    if (c->profiling == 2) return xcg::tl_finish(c, (cudaStream_t)stream);
+    return XCG_OK;
 }
 
 }  // extern "C"
@@ -473,7 +485,7 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     if (tcf || P.corr_mode < 2) P.rc = 0;
     const bool rc = P.rc != 0;
     const int nk = (tcf ? 6 : 4) - (P.interp_flag ? 0 : 1);
-    if (c->profiling) {
+    if (c->profiling == 1) {
         const size_t need = (size_t)nb * nk * 2 + (size_t)nb * 2;   // + the planners' own pair
         while (c->events.size() < need) {
             cudaEvent_t ev;
@@ -488,7 +500,8 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     // batches alternate between the scratch slots on the slot streams (forked
     // from and joined back into s); profiling runs them in order on s so each
     // kernel's events time that kernel alone
-    const bool fork = nb > 1 && c->nslots > 1 && !c->profiling;
+    const bool fork = nb > 1 && c->nslots > 1 && c->profiling != 1;
+    const bool tl = c->profiling == 2;
     for (int b = 0; b < nb; b++)           // before anything is enqueued
         if (starts[b + 1] - starts[b] > c->max_batch) {
             set_last_error("batch larger than the context's scratch");
@@ -526,7 +539,7 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
         Q.locs = locs0 + Q.win0;
         Q.winref = ref0 ? ref0 + Q.win0 : nullptr;
         for (int k = 0; k < nk; k++) {
-            if (c->profiling) cudaEventRecord(c->events[ei++], ss);
+            if (c->profiling == 1) cudaEventRecord(c->events[ei++], ss);
             const bool tm = Q.corr_mode < 2;     // -time / -time4: full-search surface
             if (k == 0 && rows) {
                 const xcg_status rs = rows(Q, ss);
@@ -545,9 +558,9 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
                     case 0:
                         if (rc) {
                             if (b >= npre) {
-                                if (c->profiling) cudaEventRecord(c->events[pe], ss);
+                                if (c->profiling == 1) cudaEventRecord(c->events[pe], ss);
                                 launch_rc_plan(Q, ss);
-                                if (c->profiling) cudaEventRecord(c->events[pe + 1], ss);
+                                if (c->profiling == 1) cudaEventRecord(c->events[pe + 1], ss);
                                 pe += 2;
                             }
                             launch_segrows(Q, ss);
@@ -565,10 +578,11 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
                     case 3: launch_subpix(Q, ss); break;
                 }
             }
-            if (c->profiling) cudaEventRecord(c->events[ei++], ss);
+            if (c->profiling == 1) cudaEventRecord(c->events[ei++], ss);
+            if (tl) XCG_TRY_ST(tl_mark(c, ss, 1000 + 10 * b + k));
             c->stats.launches++;
         }
-        if (c->profiling && rc) {     // the chunks this batch's row stage computed (profiling synchronises anyway)
+        if (c->profiling == 1 && rc) {     // the chunks this batch's row stage computed (profiling synchronises anyway)
             int n = 0;
             XCG_CK(cudaMemcpyAsync(&n, Q.rc_count, sizeof(int), cudaMemcpyDeviceToHost, ss), "read chunk count");
             XCG_CK(cudaStreamSynchronize(ss), "cudaStreamSynchronize");
@@ -581,12 +595,13 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
             XCG_CK(cudaStreamWaitEvent(s, c->ev_join[k], 0), "cudaStreamWaitEvent");
         }
     }
+    if (tl) XCG_TRY_ST(tl_mark(c, s, 2));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     c->stats.batches += nb;
     c->stats.batch_windows = maxw;
     c->stats.nkernels = nk;
-    if (c->profiling) {
+    if (c->profiling == 1) {
         XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
         ei = 0;
         for (int b = 0; b < nb; b++)
@@ -605,6 +620,32 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     return XCG_OK;
 }
 
+xcg_status tl_mark(xcg_ctx *c, cudaStream_t ss, int tag) {
+    const size_t i = c->tl_tags.size();
+    if (i >= 64) return XCG_OK;                  // the stats hold 64 marks
+    if (c->tl_events.size() <= i) {
+        cudaEvent_t ev;
+        XCG_CK(cudaEventCreate(&ev), "cudaEventCreate");
+        c->tl_events.push_back(ev);
+    }
+    XCG_CK(cudaEventRecord(c->tl_events[i], ss), "cudaEventRecord");
+    c->tl_tags.push_back(tag);
+    return XCG_OK;
+}
+
+xcg_status tl_finish(xcg_ctx *c, cudaStream_t s) {
+    XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    const int n = (int)c->tl_tags.size();
+    c->stats.timeline_n = n;
+    for (int i = 0; i < n; i++) {
+        float ms = 0.f;
+        XCG_CK(cudaEventElapsedTime(&ms, c->tl_events[0], c->tl_events[i]), "cudaEventElapsedTime");
+        c->stats.timeline_tag[i] = c->tl_tags[i];
+        c->stats.timeline_ms[i] = ms;
+    }
+    return XCG_OK;
+}
+
 }  // namespace xcg
 
 extern "C" {
@@ -617,6 +658,7 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     if (!c || nlocs < 0 || (nlocs > 0 && (!master || !slave || !locs || !results))) return XCG_ERR_ARG;
     if (m_nx <= 0 || m_ny <= 0 || s_nx <= 0 || s_ny <= 0) return XCG_ERR_ARG;
     if (nlocs == 0) return XCG_OK;
+    const auto t_entry = std::chrono::steady_clock::now();
     XCG_CK(cudaSetDevice(c->device), "cudaSetDevice");
     const size_t es = 4;     // bytes per sample: an int16 I/Q pair or a float32
     const size_t need[2] = {(size_t)m_nx * m_ny * es, (size_t)s_nx * s_ny * es};
@@ -644,6 +686,8 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     cudaStream_t s = c->stream;
     XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");      // the staging buffer is free again
     memcpy(h_locs, locs, (size_t)nlocs * sizeof(xcg_loc));
+    c->tl_tags.clear();
+    if (c->profiling == 2) XCG_TRY_ST(xcg::tl_mark(c, s, 1));
     XCG_CK(cudaMemcpyAsync(c->d_locs, h_locs, (size_t)nlocs * sizeof(xcg_loc), cudaMemcpyHostToDevice, s), "copy locs");
     // Copy the images in row bands on one stream and launch the row stage of
     // each batch in sub-ranges of about XCG_ROW_SUB windows, each right after
@@ -739,6 +783,7 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
                 }
                 XCG_CK(cudaEventRecord(c->band_ready[nev], c->copy_stream), "cudaEventRecord");
                 XCG_CK(cudaStreamWaitEvent(ss, c->band_ready[nev], 0), "cudaStreamWaitEvent");
+                if (c->profiling == 2) XCG_TRY_ST(xcg::tl_mark(c, c->copy_stream, 100 + (int)nev));
                 nev++;
                 Qb.rc_band = b;
                 xcg::launch_segrows(Qb, ss);
@@ -766,6 +811,7 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
             }
             XCG_CK(cudaEventRecord(c->band_ready[nev], c->copy_stream), "cudaEventRecord");
             XCG_CK(cudaStreamWaitEvent(ss, c->band_ready[nev], 0), "cudaStreamWaitEvent");
+            if (c->profiling == 2) XCG_TRY_ST(xcg::tl_mark(c, c->copy_stream, 100 + (int)nev));
             nev++;
             xcg::launch_rows(xcg::rows_subrange(Q, o0, o1 - o0), ss);
         }
@@ -795,7 +841,11 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
         return st;
     }
     XCG_CK(cudaMemcpyAsync(h_res, c->d_res, (size_t)nlocs * sizeof(xcg_result), cudaMemcpyDeviceToHost, s), "copy results");
+    if (c->profiling == 2) XCG_TRY_ST(xcg::tl_mark(c, s, 3));
+    c->stats.host_enqueue_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_entry).count();
     XCG_CK(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (c->profiling == 2) XCG_TRY_ST(xcg::tl_finish(c, s));
     if (c->base.tc_form && c->tc_err) {     // a tensor-core wait that ran out leaves its block unwritten
         int herr = 0;
         XCG_CK(cudaMemcpy(&herr, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost), "read tensor-core status");

@@ -51,9 +51,11 @@ struct xcg_ctx {
     uint8_t *tc_prep = nullptr;
     int *tc_err = nullptr;
     int inject_tc_timeout = 0;    // xcg_debug_inject_stage_timeout: the next call sets the flag instead of clearing it
-    // profiling
+    // profiling: 1 events around each launch, 2 timeline marks
     int profiling = 0;
     std::vector<cudaEvent_t> events;
+    std::vector<cudaEvent_t> tl_events;
+    std::vector<int> tl_tags;             // marks of the current call, in order of recording
     xcg_stats stats;
 };
 
@@ -68,6 +70,10 @@ using RowsHook = std::function<xcg_status(const Plan &Q, cudaStream_t ss)>;
 // window arrays in P (locs, winref), b < nbatch; updates the context stats.
 xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nbatch, cudaStream_t s,
                       const RowsHook &rows = {});
+// Timeline mode: record mark `tag` on stream ss; tl_finish (after the call's
+// work was enqueued) waits for the device and fills the stats' timeline.
+xcg_status tl_mark(xcg_ctx *c, cudaStream_t ss, int tag);
+xcg_status tl_finish(xcg_ctx *c, cudaStream_t s);
 // Windows per batch xcg_correlate_device uses for nlocs windows.
 int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len);
 // Windows [off, off + n) of batch plan P, for a row-stage sub-launch.

@@ -58,7 +58,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_int64), ("batches", ctypes.c_int32), ("batch_windows", ctypes.c_int32),
                 ("kernel_ms", ctypes.c_double * 8), ("scratch_bytes", ctypes.c_size_t),
                 ("nkernels", ctypes.c_int32), ("pad", ctypes.c_int32), ("row_chunks", ctypes.c_int64),
-                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("host_enqueue_ms", ctypes.c_double),
+                ("timeline_n", ctypes.c_int32), ("timeline_tag", ctypes.c_int32 * 64), ("timeline_ms", ctypes.c_float * 64)]
 
 
 KERNEL_NAMES = ("k_rows", "k_cols", "k_peak", "k_subpix")
@@ -219,8 +220,15 @@ class Context:
     def __exit__(self, *a):
         self.close()
 
-    def set_profiling(self, on: bool):
-        self._L.xcg_set_profiling(self._h, 1 if on else 0)
+    def set_profiling(self, on):
+        """True/1: events around every launch, batches in order (kernel_ms); 2: timeline marks with the
+        batches overlapping (timeline()); False/0: off."""
+        self._L.xcg_set_profiling(self._h, 2 if on == 2 else (1 if on else 0))
+
+    def timeline(self):
+        """[(tag, ms)] of the last call in timeline mode (tags: include/xcorr_gb300.h, xcg_stats)."""
+        st = self.stats()
+        return [(int(st.timeline_tag[i]), float(st.timeline_ms[i])) for i in range(st.timeline_n)]
 
     def set_dft_form(self, form: int):
         """0: FP32 SIMT FFTs (default); 1: split-FP16 tensor-core DFTs (precision form)."""

@@ -97,6 +97,14 @@ typedef struct {
     int64_t h2d_bytes;         /* xcg_correlate: bytes copied host to device (the image rows and columns
                                   the windows read, the locations); 0 for the device entries */
     int64_t d2h_bytes;         /* xcg_correlate: bytes copied device to host (the result records) */
+    double host_enqueue_ms;    /* xcg_correlate: host time from entry until every copy and launch was
+                                  enqueued (the rest of the call waits for the device) */
+    /* timeline (xcg_set_profiling(ctx, 2)): device times, ms after the call's first device work, at which
+       each mark was passed; tags: 1 start, 2 every batch joined, 3 results on the host, 100 + i image band
+       i copied (host entry), 1000 + 10 b + k stage k of batch b done (the stages of kernel_ms) */
+    int32_t timeline_n;
+    int32_t timeline_tag[64];
+    float timeline_ms[64];
 } xcg_stats;
 
 const char *xcg_status_string(xcg_status s);
@@ -339,8 +347,10 @@ xcg_status xcg_tc_gemm_check(int32_t m_tiles, int32_t n_tile, int32_t k, int32_t
  * counterpart in the reference. */
 xcg_status xcg_fp32_fma_rate(int32_t device, double *tflops);
 
-/* Record CUDA events around every kernel launch (adds a synchronisation at
- * the end of each correlate call to read them). */
+/* 1: record CUDA events around every kernel launch, the batches run one
+ * after another (adds a synchronisation at the end of each correlate call to
+ * read them; kernel_ms).  2: timeline, the batches overlapping as usual, an
+ * event after every stage and image band (timeline_*).  0: off. */
 void xcg_set_profiling(xcg_ctx *ctx, int32_t enable);
 void xcg_get_stats(const xcg_ctx *ctx, xcg_stats *out);
 

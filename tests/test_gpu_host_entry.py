@@ -116,3 +116,27 @@ def test_random_geometry(seed):
         r = ctx.correlate(m, s, locs, 0, y_offset, ast, strip_len=nxl)
         d = _device(ctx, m, s, locs, nxl, y_offset, ast)
     _same(r, d)
+
+
+def test_timeline_marks(pairs):
+    """Timeline mode (xcg_set_profiling 2): the batches still overlap, the
+    results are the same bits, and the marks come in the order each stream
+    passed them: every image band, each batch's stages in order, then the
+    join and the results."""
+    (m1, s1), _ = pairs
+    locs = xg.grid(1024, 3072, 16, 40, 64, 64)                    # 640 windows: two batches
+    with xg.Context(xg.params(64, 64)) as ctx:
+        plain = ctx.correlate(m1, s1, locs, strip_len=16)
+        ctx.set_profiling(2)
+        timed = ctx.correlate(m1, s1, locs, strip_len=16)
+        tl = dict(ctx.timeline())
+        st = ctx.stats()
+    _same(plain, timed)
+    assert st.batches == 2
+    assert tl[1] == 0.0 and tl[3] >= tl[2] > 0.0
+    bands = sorted(t for t in tl if 100 <= t < 1000)
+    assert bands == list(range(100, 100 + len(bands))) and len(bands) >= 2
+    assert all(tl[a] <= tl[b] for a, b in zip(bands, bands[1:]))          # one copy stream
+    for b in range(st.batches):
+        stages = [tl[1000 + 10 * b + k] for k in range(4)]
+        assert stages == sorted(stages) and stages[-1] <= tl[2]
