@@ -953,13 +953,13 @@ static void launch_cols_rc_t(const Plan &P, cudaStream_t s) {
         k_cols_rc<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
         return;
     }
-    // persistent: one CTA per resident slot (cols_cfg 2: one slot per SM left
-    // to the other scratch slot's kernels), tiles split into contiguous ranges
+    // persistent: one CTA per resident slot, tiles split into contiguous
+    // ranges (leaving one slot per SM to the other batch's kernels measured
+    // the same on the device entry and slower on the host entry)
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int per_sm = (P.cols_cfg == 2 && G::BLOCKS > 1) ? G::BLOCKS - 1 : G::BLOCKS;
-    const int grid = std::min(ntiles, sms * per_sm);
+    const int grid = std::min(ntiles, sms * G::BLOCKS);
     k_cols_rcp<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
 }
 void launch_cols_rc(const Plan &P, cudaStream_t s) {

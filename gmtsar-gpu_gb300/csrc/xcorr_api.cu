@@ -467,7 +467,10 @@ int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len) {
     // one-CTA-per-SM tensor stages: 626 K against 601 K windows/s) and on
     // shared row segments (the second batch's row stage overlaps the first's
     // column stage: 0.548 against 0.563 ms per 1000 windows of 128x128, and
-    // in the host entry its image copy too: 0.732 against 0.791 ms).
+    // in the host entry its image copy too: 0.732 against 0.791 ms).  On the
+    // host entry a first batch of a quarter of the windows measured the same
+    // as two halves (0.702 against 0.703 ms per call): the call's timeline
+    // shows the device busy from the end of the first batch's row stage on.
     int bw = c->max_batch;
     if ((c->base.tc_form || c->base.rc) && nlocs >= 512 && (nlocs + 1) / 2 < bw) bw = (nlocs + 1) / 2;
     if (strip_len > 0 && strip_len <= bw) bw = ((bw + strip_len - 1) / strip_len) * strip_len;   // whole strips
