@@ -181,7 +181,10 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
             for (int c = c0 + l32; c < c1; c += 32) P.rc_desc[c] = make_int4(pidx, img, x0, y0 + (c - c0) * rpc);
         }
     }
-    if (tid == 0) *P.rc_count = total;
+    if (tid == 0) {
+        *P.rc_count = total;
+        if (P.rc_tile_next) *P.rc_tile_next = 0;  // the persistent column stage's tile counter
+    }
     if (P.rc_nbands > 0) {
         // the chunks listed band by band (order within a band is free).  A
         // chunk belongs to the first band whose end row lies beyond its last
@@ -661,13 +664,31 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
     float2 *boxy = cols + (2 * CP + 1) * CS;    // [M] DFT of the row mask
     float2 *boxx = boxy + M;                    // [CP + 1] DFT of the column mask at this tile's kx, then N/2
     double *dsum = reinterpret_cast<double *>(boxx + CP + 1);   // [4] per-warp partial chunk sums
+    int *grab = reinterpret_cast<int *>(dsum + 4);              // [1] the next chunk of tiles (thread 0's grab)
 
     const int N = P.npx, NH = N / 2;
     const int NG = NH / CP;                     // column groups per window
     const int ntiles = P.nwin * NG;
-    const int t0 = (int)((long long)ntiles * blockIdx.x / gridDim.x);
-    const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
-    if (t0 >= t1) return;
+    // Tiles come in chunks of a quarter window from a counter the planner
+    // zeroed (a CTA that starts late, behind the other batch's kernels, takes
+    // fewer), or, without the counter, as one contiguous range per CTA.
+    const bool dyn = (P.rc_tile_next != nullptr);
+    const int K = (NG >= 4) ? NG / 4 : 1;
+    int t, tend;                                // the current chunk [t, tend)
+    if (dyn) {
+        if (threadIdx.x == 0) *grab = atomicAdd(P.rc_tile_next, K);
+        __syncthreads();
+        t = *grab;
+        __syncthreads();                        // every thread has read it before the next grab
+    } else {
+        t = (int)((long long)ntiles * blockIdx.x / gridDim.x);
+        tend = (int)((long long)ntiles * (blockIdx.x + 1) / gridDim.x);
+        if (t >= tend) return;
+    }
+    if (dyn) {
+        if (t >= ntiles) return;
+        tend = min(t + K, ntiles);
+    }
     const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
     const int lane = l32 % T;
     const int team = warp * (32 / T) + l32 / T;
@@ -706,16 +727,18 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
         cp_async_commit();
     };
 
-    stage_slave(t0);
-    stage_master(t0);
+    stage_slave(t);
+    stage_master(t);
     for (int i = threadIdx.x; i < TWL; i += THR) tw[i] = P.tw_col[i];
     for (int i = threadIdx.x; i < M; i += THR) boxy[i] = __ldg(P.box_y + i);
 
     int cur_w = -1;
     float dc1 = 0.f, m2 = 0.f;
-    for (int t = t0; t < t1; t++) {
+    for (;;) {
         int w, b;
         tile(t, w, b);
+        // the last tile of a chunk: the next chunk, read after the barrier below
+        if (dyn && t + 1 == tend && threadIdx.x == 0) *grab = atomicAdd(P.rc_tile_next, K);
         const int kx0 = b * CP;
         const bool neww = (w != cur_w);
         // (the previous tile's last barrier ordered every read of boxx and dsum before these writes)
@@ -731,7 +754,10 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
             if (l32 == 0) dsum[warp] = sp;
         }
         cp_async_wait<1>();                      // this tile's slave rows in (this thread's copies)
-        __syncthreads();                         // ... and everyone's; boxx, dsum, tw, boxy written
+        __syncthreads();                         // ... and everyone's; boxx, dsum, tw, boxy, grab written
+        int tn = -1;                             // the next tile, none: -1
+        if (t + 1 < tend) tn = t + 1;
+        else if (dyn && *grab < ntiles) tn = *grab;
         if (neww) {
             const double inv = pow2_inv(N * M);
             const double s1 = (dsum[0] + dsum[1]) * inv, s2 = (dsum[2] + dsum[3]) * inv;
@@ -777,7 +803,7 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
                 z[m] = product(kx, z[m], pa[fft_pad(ky)], ky);
             }
             __syncthreads();                     // every team has read its slave column
-            if (t + 1 < t1) stage_slave(t + 1);
+            if (tn >= 0) stage_slave(tn);
             team_fft_reg<M, +1>(z, a, tw, lane);
 #pragma unroll
             for (int m = PER / 4; m < 3 * PER / 4; m++) a[fft_pad(lane + T * m)] = z[m];
@@ -838,10 +864,11 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
                     qw[(size_t)yq * P.qpitch + NH] = cols[CP * CS + fft_pad(yq + M / 4)];
         }
         __syncthreads();                         // the slots are read: the next tile's rows may land
-        if (t + 1 < t1) {
-            if (b == 0) stage_slave(t + 1);
-            stage_master(t + 1);
-        }
+        if (tn < 0) break;
+        if (b == 0) stage_slave(tn);
+        stage_master(tn);
+        if (tn != t + 1) tend = min(tn + K, ntiles);
+        t = tn;
     }
 }
 
@@ -863,7 +890,7 @@ template <int M>
 static size_t cols_rc_smem() {
     using G = ColsGeom<M, 128>;
     return G::TWL * sizeof(float2) + (size_t)(2 * G::CP + 1) * G::CS * sizeof(float2) +
-           (size_t)(M + G::CP + 1) * sizeof(float2) + 4 * sizeof(double);
+           (size_t)(M + G::CP + 1) * sizeof(float2) + 4 * sizeof(double) + 16;
 }
 
 template <int N>

@@ -160,7 +160,7 @@ static size_t per_window_bytes(const xcg::Plan &B) {
     const size_t ch = (size_t)2 * B.nchunks;
     s += align256(ch * sizeof(int4)) + align256(sizeof(int2)) + align256(sizeof(int)) + align256(ch * 1024 * sizeof(float)) +
          align256(ch * 512 * sizeof(float2)) + align256(ch * sizeof(float)) + align256(ch * sizeof(float2)) + align256(ch) +
-         align256(ch * sizeof(int)) + align256(sizeof(int));
+         align256(ch * sizeof(int)) + align256(sizeof(int)) + align256(sizeof(int));
     return s;
 }
 
@@ -289,6 +289,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         c->off_rc_oob = take(ch);
         c->off_rc_order = take(ch * sizeof(int));
         c->off_rc_band_start = take(sizeof(int));       // 9 ints: one 256-byte block at least
+        c->off_rc_tile_next = take(sizeof(int));
         c->slot_bytes = align256(off);
         c->scratch_bytes = c->slot_bytes * (size_t)c->nslots;
         XCG_CK_C(cudaMalloc(&c->d_scratch, c->scratch_bytes), "cudaMalloc scratch");
@@ -425,6 +426,7 @@ Plan ctx_plan(const xcg_ctx *c) {
     P.rc_oob = (unsigned char *)(sc + c->off_rc_oob);
     P.rc_order = (int *)(sc + c->off_rc_order);
     P.rc_band_start = (int *)(sc + c->off_rc_band_start);
+    P.rc_tile_next = (int *)(sc + c->off_rc_tile_next);
     return P;
 }
 
@@ -437,7 +439,7 @@ static Plan with_slot(Plan P, size_t off) {
     P.surf = mv(P.surf); P.md = mv(P.md); P.mdnext = mv(P.mdnext); P.corr0n = mv(P.corr0n);
     P.rc_desc = mv(P.rc_desc); P.rc_wch = mv(P.rc_wch); P.rc_count = mv(P.rc_count); P.rc_amp = mv(P.rc_amp);
     P.rc_spec = mv(P.rc_spec); P.rc_part = mv(P.rc_part); P.rc_minmax = mv(P.rc_minmax); P.rc_oob = mv(P.rc_oob);
-    P.rc_order = mv(P.rc_order); P.rc_band_start = mv(P.rc_band_start);
+    P.rc_order = mv(P.rc_order); P.rc_band_start = mv(P.rc_band_start); P.rc_tile_next = mv(P.rc_tile_next);
     return P;
 }
 

@@ -32,7 +32,7 @@ struct xcg_ctx {
         off_mdnext, off_corr0n;
     // shared row segments (segment_rows.cu): chunk arrays per slot
     size_t off_rc_desc, off_rc_wch, off_rc_count, off_rc_amp, off_rc_spec, off_rc_part, off_rc_minmax, off_rc_oob,
-        off_rc_order, off_rc_band_start;
+        off_rc_order, off_rc_band_start, off_rc_tile_next;
     // host-entry buffers
     void *d_img[2] = {nullptr, nullptr};
     size_t img_bytes[2] = {0, 0};

@@ -100,6 +100,7 @@ struct Plan {
     int rc_band_end[2][8];  // master / slave rows [.., end) of each band
     int *rc_order;          // [chunks] chunk indices band by band
     int *rc_band_start;     // [9] first entry of each band in rc_order, then the total
+    int *rc_tile_next;      // [1] the persistent column stage's next tile (zeroed by the planner), or null
 };
 
 // The pair of batch window w (a copy: taking the address of the kernel
