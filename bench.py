@@ -301,8 +301,9 @@ def frame_measure(steps, warmup, max_batch=0, e2e_calls=3):
             "config": {"workload": "full frame", "image": "10240x30720 complex int16, varying shift, 20 dB",
                        "windows": nwin, "xsearch": 128, "ysearch": 128, "range_interp": 2, "interp": 16,
                        "l2": "flushed between steps (256 MB write)", "generation_s": gen_s},
-            "kernel_ms_per_step": {n: st.kernel_ms[i] for i, n in
-                                   enumerate(xg.RC_KERNEL_NAMES if st.row_chunks > 0 else xg.KERNEL_NAMES)},
+            "kernel_ms_per_step": {n: st.kernel_ms[i] - (st.kernel_ms[7] if (i == 0 and st.row_chunks > 0) else 0.0)
+                                   for i, n in enumerate(xg.RC_KERNEL_NAMES if st.row_chunks > 0 else xg.KERNEL_NAMES)},
+            "planner_ms_per_step": st.kernel_ms[7] if st.row_chunks > 0 else 0.0,
             "row_chunks_per_step": int(st.row_chunks),
             "batches_per_step": st.batches,
             "e2e": {"value": nwin / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(e2e_st.h2d_bytes),
@@ -426,7 +427,8 @@ def run_stack(args):
                             "bucket_npx": [int(st.bucket_npx[i]) for i in range(st.buckets)],
                             "bucket_batch": [int(st.bucket_batch[i]) for i in range(st.buckets)],
                             "bucket_cols_cfg": [int(st.bucket_cols_cfg[i]) for i in range(st.buckets)],
-                            "bucket_peak_cfg": [int(st.bucket_peak_cfg[i]) for i in range(st.buckets)]},
+                            "bucket_peak_cfg": [int(st.bucket_peak_cfg[i]) for i in range(st.buckets)],
+                            "bucket_row_sharing": [int(st.bucket_row_sharing[i]) for i in range(st.buckets)]},
             "eager_ms_per_step": eager_ms, "graph_ms_per_step": ms / args.steps,
             "clocks": clk}
     print(json.dumps(line), flush=True)
@@ -626,6 +628,8 @@ def run_ours(args):
         plan_ms += st.kernel_ms[7]
     ctx.set_profiling(False)
     nprof = max(3, min(args.steps, 20))
+    if row_chunks > 0:
+        kms[0] -= plan_ms               # the row kernel alone: the planners have their own entry
     row_chunks /= nprof                 # 1024-sample chunks the row stage computed per step (0: per-window rows)
     # the FP32 SIMT ceiling of the roofline, measured on this GPU by the library's FMA kernel
     try:
@@ -772,7 +776,7 @@ def run_ours(args):
         if world == 1 and not args.no_frame:
             fr = frame_measure(3, 3, e2e_calls=3)
             line["frame"] = {k: fr[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup",
-                                                 "kernel_ms_per_step", "e2e", "clocks")}
+                                                 "kernel_ms_per_step", "planner_ms_per_step", "e2e", "clocks")}
             line["frame"]["windows"] = fr["config"]["windows"]
         if world == 1 and not args.no_programs:
             line["programs"] = program_times()
