@@ -105,14 +105,21 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
     int *wsum = rtail + RC_ENTRIES;                            // [72] scan scratch
 
     const int tid = threadIdx.x;
-    const int nent = 2 * P.nwin;
+    // Two CTAs (no row bands): CTA i plans image i's entries alone, its runs
+    // never meeting the other image's, and numbers its chunks from
+    // i * nwin * nchunks (the most chunks the master entries can need), so
+    // neither waits for the other's total.  One CTA: both images.
+    const bool split = (gridDim.x == 2);
+    const int nent = split ? P.nwin : 2 * P.nwin;
+    const int cbase = (split && blockIdx.x == 1) ? P.nwin * P.nchunks : 0;
     const int npx = P.npx, npy = P.npy, rpc = P.rpc;
     int n = 2;
     while (n < nent) n <<= 1;
     for (int e = tid; e < RC_ENTRIES; e += PLAN_THREADS) {
         unsigned long long k = ~0ull;             // padding sorts last
+        const int ge = split ? 2 * e + (int)blockIdx.x : e;    // the entry: 2 w + image
         if (e < nent) {
-            const int w = e >> 1, img = e & 1;
+            const int w = ge >> 1, img = ge & 1;
             const xcg_loc loc = P.locs[w];
             int local, pidx;
             const PairDev pd = pair_of(P, w, local, pidx);
@@ -124,7 +131,7 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
                 (unsigned long long)(y0 + KEY_Y_BIAS);
         }
         key[e] = k;
-        pay[e] = e;
+        pay[e] = ge;
         rlen[e] = 0;
     }
     __syncthreads();
@@ -167,7 +174,7 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
     for (int i = tid; i < nent; i += PLAN_THREADS) {
         const int r = cnt[i] + (is_head(i) ? 0 : -1);
         const int c0 = rlen[r] + (key_y(key[i]) - key_y(key[rhead[r]])) / rpc;
-        reinterpret_cast<int *>(P.rc_wch)[pay[i]] = c0;   // rc_wch[w].x for the master, .y for the slave
+        reinterpret_cast<int *>(P.rc_wch)[pay[i]] = cbase + c0;   // rc_wch[w].x for the master, .y for the slave
     }
     // chunk descriptors: one warp per run, its lanes writing consecutive chunks
     {
@@ -178,12 +185,18 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
             const int x0 = (int)((k >> 28) & ((1u << 20) - 1)) - KEY_X_BIAS;
             const int y0 = key_y(k);
             const int c0 = rlen[r], c1 = (r + 1 < nruns) ? rlen[r + 1] : total;
-            for (int c = c0 + l32; c < c1; c += 32) P.rc_desc[c] = make_int4(pidx, img, x0, y0 + (c - c0) * rpc);
+            for (int c = c0 + l32; c < c1; c += 32) P.rc_desc[cbase + c] = make_int4(pidx, img, x0, y0 + (c - c0) * rpc);
         }
     }
     if (tid == 0) {
-        *P.rc_count = total;
-        if (P.rc_tile_next) *P.rc_tile_next = 0;  // the persistent column stage's tile counter
+        // chunks of the master entries' numbering, then of the slave's (from nwin * nchunks)
+        if (split) {
+            P.rc_count[blockIdx.x] = total;
+        } else {
+            P.rc_count[0] = total;
+            P.rc_count[1] = 0;
+        }
+        if (P.rc_tile_next && blockIdx.x == 0) *P.rc_tile_next = 0;   // the persistent column stage's tile counter
     }
     if (P.rc_nbands > 0) {
         // the chunks listed band by band (order within a band is free).  A
@@ -289,13 +302,16 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_s
     // this launch's chunks: all of them in planned order, or one row band's
     const bool banded = P.rc_nbands > 0;
     const int begin = banded ? P.rc_band_start[P.rc_band] : 0;
-    const int end = banded ? P.rc_band_start[P.rc_band + 1] : *P.rc_count;
+    // unbanded: the first planner's chunks, then the second's from nwin * nchunks
+    const int cm = banded ? 0 : P.rc_count[0];
+    const int end = banded ? P.rc_band_start[P.rc_band + 1] : cm + P.rc_count[1];
+    const int cbase = P.nwin * P.nchunks;
     const bool iq16 = (P.format == 0);
 
     // chunks are taken four per CTA, one per warp; warps share no state
     // between chunks, so a warp that runs out leaves without a barrier
     for (int i = begin + 4 * blockIdx.x + warp; i < end; i += 4 * gridDim.x) {
-        const int c = banded ? P.rc_order[i] : i;
+        const int c = banded ? P.rc_order[i] : (i < cm ? i : cbase + (i - cm));
         const int4 d = P.rc_desc[c];
         const int img = d.y;
         const PairDev *q = P.pairs ? P.pairs + d.x : nullptr;
@@ -938,7 +954,8 @@ size_t rc_max_chunks(int npx, int npy, int nwin) {
 }
 
 void launch_rc_plan(const Plan &P, cudaStream_t s) {
-    k_rc_plan<<<1, PLAN_THREADS, rc_plan_smem_bytes(), s>>>(P);
+    // one CTA per image unless the host entry wants the chunks listed by row band
+    k_rc_plan<<<P.rc_nbands > 0 ? 1 : 2, PLAN_THREADS, rc_plan_smem_bytes(), s>>>(P);
 }
 
 template <int N>

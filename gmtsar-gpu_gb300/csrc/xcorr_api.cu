@@ -588,10 +588,10 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
             c->stats.launches++;
         }
         if (c->profiling == 1 && rc) {     // the chunks this batch's row stage computed (profiling synchronises anyway)
-            int n = 0;
-            XCG_CK(cudaMemcpyAsync(&n, Q.rc_count, sizeof(int), cudaMemcpyDeviceToHost, ss), "read chunk count");
+            int n[2] = {0, 0};
+            XCG_CK(cudaMemcpyAsync(n, Q.rc_count, 2 * sizeof(int), cudaMemcpyDeviceToHost, ss), "read chunk count");
             XCG_CK(cudaStreamSynchronize(ss), "cudaStreamSynchronize");
-            c->stats.row_chunks += n;
+            c->stats.row_chunks += n[0] + n[1];
         }
     }
     if (fork) {

@@ -86,7 +86,7 @@ struct Plan {
     int rpc;                // rows per chunk: 1024 / npx
     int4 *rc_desc;          // [chunks] (pair, 0 master / 1 slave, first column, first row)
     int2 *rc_wch;           // [nwin] first master (x) and slave (y) chunk of each window
-    int *rc_count;          // chunks of the batch (written by the planner)
+    int *rc_count;          // [2] chunks of the batch (the planner): numbered from 0, then from nwin * nchunks
     float *rc_amp;          // [chunks][rpc][npx] amplitudes of the kept fine samples
     float2 *rc_spec;        // [chunks][rpc][npx/2] half row spectra; bin 0 holds (DC, Nyquist)
     float *rc_part;         // [chunks] FP32 chunk sums in the reference's tree order
