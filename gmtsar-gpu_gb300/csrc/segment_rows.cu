@@ -55,13 +55,15 @@ constexpr int KEY_Y_BITS = 24;
 constexpr int KEY_Y_BIAS = 1 << 23;
 constexpr int KEY_X_BIAS = 1 << 19;
 
-// In-place exclusive scan of a[0, RC_ENTRIES) by the whole CTA; returns the total.
-__device__ int block_exclusive_scan(int *a, int *wsum) {
+// In-place exclusive scan of a[0, ns) by the whole CTA (ns a multiple of
+// PLAN_THREADS up to RC_ENTRIES); returns the total.
+__device__ int block_exclusive_scan(int *a, int *wsum, int ns) {
     const int t = threadIdx.x, l32 = t & 31, wp = t >> 5;
+    const int per = ns / PLAN_THREADS;
     int v[PER_THREAD];
     int s = 0;
 #pragma unroll
-    for (int k = 0; k < PER_THREAD; k++) { v[k] = a[t * PER_THREAD + k]; s += v[k]; }
+    for (int k = 0; k < PER_THREAD; k++) { v[k] = (k < per) ? a[t * per + k] : 0; s += v[k]; }
     int inc = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -84,7 +86,8 @@ __device__ int block_exclusive_scan(int *a, int *wsum) {
     __syncthreads();
     int run = wsum[32 + wp] + inc - s;
 #pragma unroll
-    for (int k = 0; k < PER_THREAD; k++) { a[t * PER_THREAD + k] = run; run += v[k]; }
+    for (int k = 0; k < PER_THREAD; k++)
+        if (k < per) { a[t * per + k] = run; run += v[k]; }
     const int total = wsum[64];
     __syncthreads();
     return total;
@@ -115,7 +118,8 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
     const int npx = P.npx, npy = P.npy, rpc = P.rpc;
     int n = 2;
     while (n < nent) n <<= 1;
-    for (int e = tid; e < RC_ENTRIES; e += PLAN_THREADS) {
+    const int ns = n > PLAN_THREADS ? n : PLAN_THREADS;   // the entries the loops and scans cover
+    for (int e = tid; e < ns; e += PLAN_THREADS) {
         unsigned long long k = ~0ull;             // padding sorts last
         const int ge = split ? 2 * e + (int)blockIdx.x : e;    // the entry: 2 w + image
         if (e < nent) {
@@ -156,9 +160,9 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
     auto is_head = [&](int i) {
         return i == 0 || (key[i] >> KEY_Y_BITS) != (key[i - 1] >> KEY_Y_BITS) || key_y(key[i]) > key_y(key[i - 1]) + npy;
     };
-    for (int i = tid; i < RC_ENTRIES; i += PLAN_THREADS) cnt[i] = (i < nent && is_head(i)) ? 1 : 0;
+    for (int i = tid; i < ns; i += PLAN_THREADS) cnt[i] = (i < nent && is_head(i)) ? 1 : 0;
     __syncthreads();
-    const int nruns = block_exclusive_scan(cnt, wsum);
+    const int nruns = block_exclusive_scan(cnt, wsum, ns);
     for (int i = tid; i < nent; i += PLAN_THREADS) {
         const bool h = is_head(i);
         const int r = cnt[i] + (h ? 0 : -1);
@@ -170,7 +174,7 @@ __global__ void __launch_bounds__(PLAN_THREADS, 1) k_rc_plan(Plan P) {
     for (int r = tid; r < nruns; r += PLAN_THREADS)
         rlen[r] = (key_y(key[rtail[r]]) - key_y(key[rhead[r]]) + npy) / rpc;
     __syncthreads();
-    const int total = block_exclusive_scan(rlen, wsum);   // rlen[r] <- first chunk of run r
+    const int total = block_exclusive_scan(rlen, wsum, ns);   // rlen[r] <- first chunk of run r
     for (int i = tid; i < nent; i += PLAN_THREADS) {
         const int r = cnt[i] + (is_head(i) ? 0 : -1);
         const int c0 = rlen[r] + (key_y(key[i]) - key_y(key[rhead[r]])) / rpc;
