@@ -145,23 +145,25 @@ void xcg_default_params(xcg_params *p) {
 }
 
 static size_t per_window_bytes(const xcg::Plan &B) {
-    size_t s = 0;
-    s += align256((size_t)B.npy * B.npx * sizeof(float2));
-    s += align256((size_t)B.npy * B.npx * sizeof(float));
-    s += align256((size_t)B.ny_corr * B.nx_corr * sizeof(float));
-    s += align256((size_t)2 * B.nchunks * sizeof(float));
-    s += align256((size_t)B.nchunks);
-    s += align256((size_t)4 * B.nchunks * sizeof(float));
-    s += align256(2 * sizeof(double));
-    s += align256((size_t)B.nyc * B.qpitch * sizeof(float2));
-    s += align256((size_t)B.nyc * B.nxc * sizeof(float));
-    s += align256(64 * sizeof(float)) + align256(64) + align256(sizeof(double));
+    // the arrays every form uses
+    size_t common = align256(2 * sizeof(double));
+    common += align256((size_t)B.nyc * B.qpitch * sizeof(float2));
+    common += align256((size_t)B.nyc * B.nxc * sizeof(float));
+    common += align256(64 * sizeof(float)) + align256(64) + align256(sizeof(double));
+    // one row stage per window
+    size_t pw = align256((size_t)B.npy * B.npx * sizeof(float2));
+    pw += align256((size_t)B.npy * B.npx * sizeof(float));
+    pw += align256((size_t)B.ny_corr * B.nx_corr * sizeof(float));
+    pw += align256((size_t)2 * B.nchunks * sizeof(float));
+    pw += align256((size_t)B.nchunks);
+    pw += align256((size_t)4 * B.nchunks * sizeof(float));
     // shared row segments: at most 2 * nchunks chunks per window
     const size_t ch = (size_t)2 * B.nchunks;
-    s += align256(ch * sizeof(int4)) + align256(sizeof(int2)) + align256(sizeof(int)) + align256(ch * 1024 * sizeof(float)) +
-         align256(ch * 512 * sizeof(float2)) + align256(ch * sizeof(float)) + align256(ch * sizeof(float2)) + align256(ch) +
-         align256(ch * sizeof(int)) + align256(sizeof(int)) + align256(sizeof(int));
-    return s;
+    const size_t rc = align256(ch * sizeof(int4)) + align256(sizeof(int2)) + align256(sizeof(int)) +
+                      align256(ch * 1024 * sizeof(float)) + align256(ch * 512 * sizeof(float2)) +
+                      align256(ch * sizeof(float)) + align256(ch * sizeof(float2)) + align256(ch) +
+                      align256(ch * sizeof(int)) + align256(sizeof(int)) + align256(sizeof(int));
+    return common + (pw > rc ? pw : rc);      // a batch uses one of the two row-stage layouts
 }
 
 xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xcg_ctx **out) {
@@ -253,11 +255,14 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         XCG_CK_C(xcg::segrows_setup(B), "kernel attributes");
         if (B.corr_mode < 2) XCG_CK_C(xcg::time_setup(B), "kernel attributes");
 
-        // scratch: up to max_batch windows, at most 8 GiB or 40% of free memory
+        // scratch: up to max_batch windows, at most 32 GiB or 40% of free
+        // memory (shared row segments share more rows in larger batches: the
+        // full frame's 512-row patches need x1.6 fewer row chunks in
+        // 2000-window batches than in 500-window ones)
         const size_t pw = per_window_bytes(B);
         size_t freeb = 0, totb = 0;
         XCG_CK_C(cudaMemGetInfo(&freeb, &totb), "cudaMemGetInfo");
-        size_t budget = (size_t)8 << 30;
+        size_t budget = (size_t)32 << 30;
         if (budget > freeb * 2 / 5) budget = freeb * 2 / 5;
         // at most RC_MAX_WINDOWS windows per batch: the row-segment planner's capacity
         int mb = max_batch > 0 ? std::min(max_batch, xcg::RC_MAX_WINDOWS) : xcg::RC_MAX_WINDOWS;
@@ -266,18 +271,24 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         c->max_batch = mb;
         size_t off = 0;
         auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes * (size_t)mb); return o; };
-        c->off_zrow = take((size_t)B.npy * B.npx * sizeof(float2));
-        c->off_amp1 = take((size_t)B.npy * B.npx * sizeof(float));
-        c->off_amp2c = take((size_t)B.ny_corr * B.nx_corr * sizeof(float));
-        c->off_part = take((size_t)2 * B.nchunks * sizeof(float));
-        c->off_oob = take((size_t)B.nchunks);
-        c->off_minmax = take((size_t)4 * B.nchunks * sizeof(float));
         c->off_means = take(2 * sizeof(double));
         c->off_qspec = take((size_t)B.nyc * B.qpitch * sizeof(float2));
         c->off_surf = take((size_t)B.nyc * B.nxc * sizeof(float));
         c->off_md = take(64 * sizeof(float));
         c->off_mdnext = take(64);
         c->off_corr0n = take(sizeof(double));
+        // the two row-stage layouts share one region: one row stage per
+        // window (per-window arrays), or shared row segments (chunk arrays);
+        // a batch uses one of them, and a slot's next batch starts after it
+        const size_t region = off;
+        c->off_zrow = take((size_t)B.npy * B.npx * sizeof(float2));
+        c->off_amp1 = take((size_t)B.npy * B.npx * sizeof(float));
+        c->off_amp2c = take((size_t)B.ny_corr * B.nx_corr * sizeof(float));
+        c->off_part = take((size_t)2 * B.nchunks * sizeof(float));
+        c->off_oob = take((size_t)B.nchunks);
+        c->off_minmax = take((size_t)4 * B.nchunks * sizeof(float));
+        const size_t end_pw = off;
+        off = region;
         const size_t ch = (size_t)2 * B.nchunks;        // chunks per window at most
         c->off_rc_desc = take(ch * sizeof(int4));
         c->off_rc_wch = take(sizeof(int2));
@@ -290,6 +301,7 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         c->off_rc_order = take(ch * sizeof(int));
         c->off_rc_band_start = take(sizeof(int));       // 9 ints: one 256-byte block at least
         c->off_rc_tile_next = take(sizeof(int));
+        if (off < end_pw) off = end_pw;
         c->slot_bytes = align256(off);
         c->scratch_bytes = c->slot_bytes * (size_t)c->nslots;
         XCG_CK_C(cudaMalloc(&c->d_scratch, c->scratch_bytes), "cudaMalloc scratch");
