@@ -248,20 +248,23 @@ def _timed(step, flush, stream, steps, warmup, clocks=None):
     return sum(a.elapsed_time(b) for a, b in ev)
 
 
-def frame_measure(steps, warmup, max_batch=0, e2e_calls=3):
+def frame_measure(steps, warmup, max_batch=0, e2e_calls=3, small=False):
     """Full-frame workload: 10240 x 30720 complex-int16 pair with the shift
     field dx = 2.1 + 1e-5 x - 3e-6 y, dy = -4.7 + 2e-6 x + 8e-6 y at 20 dB
     SNR, 100 x 400 = 40,000 windows of 256 x 256 (512 x 512 transforms).
+    small: the same windows on a 4096 x 4096 pair, 20 x 40 = 800 of them
+    (rows 81 apart against 74), a size an ncu capture of its kernels takes.
     Returns its JSON line (device-timed value, end-to-end value through the
     host-buffer entry, per-kernel times, clocks)."""
     import torch
     import xcorr_gb300 as xg
     from xcorr_gb300 import synth
     dev = torch.device("cuda", torch.cuda.current_device())
+    W, H, gx, gy = (4096, 4096, 20, 40) if small else (10240, 30720, 100, 400)
     t0 = time.perf_counter()
-    m, s, _ = synth.make_pair_varying(10240, 30720, synth.cfg2_shift, noise_frac=0.01, seed=2, device=dev)
+    m, s, _ = synth.make_pair_varying(W, H, synth.cfg2_shift, noise_frac=0.01, seed=2, device=dev)
     gen_s = time.perf_counter() - t0
-    locs = xg.grid(10240, 30720, 100, 400, 128, 128)
+    locs = xg.grid(W, H, gx, gy, 128, 128)
     nwin = len(locs)
     ctx = xg.Context(xg.params(128, 128), device=dev.index, max_batch=max_batch)
     dm, ds = torch.from_numpy(m).to(dev), torch.from_numpy(s).to(dev)
@@ -271,8 +274,8 @@ def frame_measure(steps, warmup, max_batch=0, e2e_calls=3):
     stream = torch.cuda.current_stream(dev)
 
     def step():
-        ctx.correlate_device(dm.data_ptr(), 10240, 30720, ds.data_ptr(), 10240, 30720, dl.data_ptr(), nwin,
-                             dr.data_ptr(), stream.cuda_stream, strip_len=100)
+        ctx.correlate_device(dm.data_ptr(), W, H, ds.data_ptr(), W, H, dl.data_ptr(), nwin,
+                             dr.data_ptr(), stream.cuda_stream, strip_len=gx)
     clocks = ClockSampler(dev.index)
     ms = _timed(step, flush, stream, steps, warmup, clocks)
     clk = clocks.clk
@@ -285,20 +288,22 @@ def frame_measure(steps, warmup, max_batch=0, e2e_calls=3):
     del dm, ds
     pm, ps = torch.from_numpy(m).pin_memory(), torch.from_numpy(s).pin_memory()
     pmn, psn = pm.numpy(), ps.numpy()
-    ctx.correlate(pmn, psn, locs, strip_len=100)
+    ctx.correlate(pmn, psn, locs, strip_len=gx)
     e2e_runs = []
     for _ in range(e2e_calls):                   # median of the calls
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        ctx.correlate(pmn, psn, locs, strip_len=100)
+        ctx.correlate(pmn, psn, locs, strip_len=gx)
         e2e_runs.append(time.perf_counter() - t1)
     e2e_s = sorted(e2e_runs)[len(e2e_runs) // 2]
     e2e_st = ctx.stats()
     ctx.close()
-    return {"metric": "xcorr windows/s, full frame, 256^2 windows (512^2 FFT)", "value": steps * nwin / (ms / 1e3),
+    return {"metric": "xcorr windows/s, full frame, 256^2 windows (512^2 FFT)" + (" (small)" if small else ""),
+            "value": steps * nwin / (ms / 1e3),
             "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "full frame", "image": "10240x30720 complex int16, varying shift, 20 dB",
+            "config": {"workload": "full frame" + (" (small)" if small else ""),
+                       "image": f"{W}x{H} complex int16, varying shift, 20 dB",
                        "windows": nwin, "xsearch": 128, "ysearch": 128, "range_interp": 2, "interp": 16,
                        "l2": "flushed between steps (256 MB write)", "generation_s": gen_s},
             "kernel_ms_per_step": {n: st.kernel_ms[i] - (st.kernel_ms[7] if (i == 0 and st.row_chunks > 0) else 0.0)
@@ -313,7 +318,8 @@ def frame_measure(steps, warmup, max_batch=0, e2e_calls=3):
 
 
 def run_frame(args):
-    print(json.dumps(frame_measure(args.steps, args.warmup, args.max_batch)), flush=True)
+    print(json.dumps(frame_measure(args.steps, args.warmup, args.max_batch, small=args.workload == "frame-small")),
+          flush=True)
 
 
 def program_times(runs=3):
@@ -794,9 +800,10 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="headline", choices=["headline", "frame", "stack"],
+    ap.add_argument("--workload", default="headline", choices=["headline", "frame", "frame-small", "stack"],
                     help="headline: the 1000-window 128x128 case (default); frame: 40,000 windows of 256x256 on "
-                         "a 10240x30720 pair; stack: 32 pairs with mixed window sizes")
+                         "a 10240x30720 pair; frame-small: 800 such windows on a 4096x4096 pair (profiler "
+                         "captures); stack: 32 pairs with mixed window sizes")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the refined-path measurement")
     ap.add_argument("--no-precision-form", action="store_true", help="skip the tensor-core DFT measurement")
@@ -809,7 +816,7 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "frame":
+    elif args.workload in ("frame", "frame-small"):
         run_frame(args)
     elif args.workload == "stack":
         run_stack(args)
