@@ -65,9 +65,12 @@ template <int M, int THR = 128>
 struct ColsGeom {
     static constexpr int T = fft_lanes(M);
     static constexpr int PADM = fft_padded_len(M);
-    static constexpr int CS = PADM + 1;
     static constexpr int THREADS = THR;
     static constexpr int CP = THREADS / T;        // column pairs per CTA = teams
+    // slot stride in float2: a multiple of 16 plus 16 / CP, so that the
+    // (slot, row) pairs a half-warp stages or copies out (CP slots x 16 / CP
+    // rows) fall in distinct bank pairs
+    static constexpr int CS = PADM + ((CP >= 16) ? 1 : 16 / CP);
     static constexpr int TWL = fft_twiddle_len(M);
     static constexpr int BLOCKS = (M >= 1024) ? (THREADS >= 256 ? 1 : 2)
                                 : (M >= 512 ? (THREADS >= 256 ? 1 : 3) : XCG_COLS_BLOCKS * 128 / THREADS);
