@@ -58,7 +58,7 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 //              first), 5 CTAs/SM (the default); 1: 256 threads (twice the
 //              column pairs per CTA), two groups; 2: 128 threads, one group
 //   k_peak  0: 4 resident CTAs/SM (64 registers, a few spills; beats 3 for
-//              transforms up to 256 points); 1: 3 CTAs/SM (85 registers)
+//              transforms up to 256 points), 3 for 512 points; 1: one fewer
 #define XCG_COLS_BLOCKS 5
 
 template <int M, int THR = 128>

@@ -943,7 +943,7 @@ static size_t cols_smem(int) {
 }
 // resident k_peak CTAs per SM for configuration cfg
 template <int N>
-constexpr int peak_minb(int cfg) { return (N <= 256) ? (cfg == 1 ? 3 : 4) : (N <= 512 ? 2 : 1); }
+constexpr int peak_minb(int cfg) { return (N <= 256) ? (cfg == 1 ? 3 : 4) : (N <= 512 ? (cfg == 1 ? 2 : 3) : 1); }
 template <int N>
 static size_t peak_smem() {
     constexpr int T = fft_lanes(N);
