@@ -814,59 +814,59 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
             if ((kxx + ky) & 1) { pr.x = -pr.x; pr.y = -pr.y; }
             return pr;
         };
+        // the product of column kx: from the master spectrum in registers, or
+        // in column group 0 (CTA-uniform) through the master slot, where the
+        // kx = 0 team splits the packed (DC, Nyquist) column and puts column
+        // N/2's product in the extra slot
+        const bool dc = (kx == 0);
+        const int nout = (b == 0 && __any_sync(0xffffffffu, dc)) ? 2 : 1;    // warp-uniform
+        float2 *xs = cols + 2 * CP * CS;
         if (b != 0) {
-            // no packed column in this tile (CTA-uniform): the product from the
-            // master spectrum in registers, then the slave slots are free
 #pragma unroll
             for (int m = 0; m < PER; m++) {
                 const int ky = lane + T * m;
                 z[m] = product(kx, z[m], pa[fft_pad(ky)], ky);
             }
-            __syncthreads();                     // every team has read its slave column
-            if (tn >= 0) stage_slave(tn);
-            team_fft_reg<M, +1>(z, a, tw, lane);
-#pragma unroll
-            for (int m = PER / 4; m < 3 * PER / 4; m++) a[fft_pad(lane + T * m)] = z[m];
         } else {
-            // column group 0: k_cols_rc's order, the kx = 0 team's second
-            // output (column N/2) through the extra slot into its slave slot
 #pragma unroll
             for (int m = 0; m < PER; m++) a[fft_pad(lane + T * m)] = z[m];
             __syncwarp();
-            const bool dc = (kx == 0);
-            const int nout = __any_sync(0xffffffffu, dc) ? 2 : 1;
-            float2 *xs = cols + 2 * CP * CS;
-#pragma unroll 1
-            for (int o = 0; o < nout; o++) {
-                if (o == 0) {
 #pragma unroll
-                    for (int m = 0; m < PER; m++) {
-                        const int ky = lane + T * m;
-                        const float2 zm = a[fft_pad(ky)], zs = pa[fft_pad(ky)];
-                        if (!dc) {
-                            z[m] = product(kx, zm, zs, ky);
-                        } else {
-                            const int kyn = (M - ky) & (M - 1);
-                            const float2 wm = a[fft_pad(kyn)], ws = pa[fft_pad(kyn)];
-                            const float2 D1 = make_float2(0.5f * (zm.x + wm.x), 0.5f * (zm.y - wm.y));
-                            const float2 D2 = make_float2(0.5f * (zs.x + ws.x), 0.5f * (zs.y - ws.y));
-                            const float2 Q1 = make_float2(0.5f * (zm.y + wm.y), -0.5f * (zm.x - wm.x));
-                            const float2 Q2 = make_float2(0.5f * (zs.y + ws.y), -0.5f * (zs.x - ws.x));
-                            z[m] = product(0, D1, D2, ky);
-                            xs[fft_pad(ky)] = product(NH, Q1, Q2, ky);
-                        }
-                    }
+            for (int m = 0; m < PER; m++) {
+                const int ky = lane + T * m;
+                const float2 zm = a[fft_pad(ky)], zs = pa[fft_pad(ky)];
+                if (!dc) {
+                    z[m] = product(kx, zm, zs, ky);
                 } else {
-#pragma unroll
-                    for (int m = 0; m < PER; m++) z[m] = xs[fft_pad(lane + T * m)];
+                    const int kyn = (M - ky) & (M - 1);
+                    const float2 wm = a[fft_pad(kyn)], ws = pa[fft_pad(kyn)];
+                    const float2 D1 = make_float2(0.5f * (zm.x + wm.x), 0.5f * (zm.y - wm.y));
+                    const float2 D2 = make_float2(0.5f * (zs.x + ws.x), 0.5f * (zs.y - ws.y));
+                    const float2 Q1 = make_float2(0.5f * (zm.y + wm.y), -0.5f * (zm.x - wm.x));
+                    const float2 Q2 = make_float2(0.5f * (zs.y + ws.y), -0.5f * (zs.x - ws.x));
+                    z[m] = product(0, D1, D2, ky);
+                    xs[fft_pad(ky)] = product(NH, Q1, Q2, ky);
                 }
-                float2 *dst = (o == 0) ? a : pa;
-                __syncwarp();
-                team_fft_reg<M, +1>(z, dst, tw, lane);
-#pragma unroll
-                for (int m = PER / 4; m < 3 * PER / 4; m++) dst[fft_pad(lane + T * m)] = z[m];
-                __syncwarp();
             }
+        }
+        __syncthreads();                         // every team has read its slave column
+        // outside column group 0 the slave slots are free: the next tile's slave rows
+        if (b != 0 && tn >= 0) stage_slave(tn);
+        // inverse of column kx into its master slot; in column group 0 the
+        // kx = 0 team's second output, column N/2, into its slave slot (one
+        // call site of the transform for both cases)
+#pragma unroll 1
+        for (int o = 0; o < nout; o++) {
+            if (o == 1) {
+#pragma unroll
+                for (int m = 0; m < PER; m++) z[m] = xs[fft_pad(lane + T * m)];
+            }
+            float2 *dst = (o == 0) ? a : pa;
+            __syncwarp();
+            team_fft_reg<M, +1>(z, dst, tw, lane);
+#pragma unroll
+            for (int m = PER / 4; m < 3 * PER / 4; m++) dst[fft_pad(lane + T * m)] = z[m];
+            __syncwarp();
         }
         __syncthreads();
         {   // rows y in [ysearch, ysearch + nyc) of the half spectrum, kx <= N/2
