@@ -13,7 +13,8 @@
 // frequency domain by linearity (k_cols_rc), so the row spectra do not depend
 // on the window either.
 //
-//   k_rc_plan   one CTA per batch: every window contributes a master and a
+//   k_rc_plan   one CTA per batch, or one per image when the chunks need no
+//               row-band order: every window contributes a master and a
 //               slave entry (pair, image, first column, first row); entries
 //               with the same pair, image, first column and first row modulo
 //               the rows of a chunk are sorted by row and merged where their
@@ -29,9 +30,9 @@
 //               the master's and the masked slave's half spectra, the
 //               product with the demean/mask corrections and the inverse
 //               column FFT of the surface rows, as k_cols; the default form
-//               (k_cols_rcp) is persistent, each CTA walking a range of
-//               (window, column group) tiles with the next tile's rows staged
-//               while the current one is transformed
+//               (k_cols_rcp) is persistent, each CTA taking (window, column
+//               group) tiles from a counter, the next tile's rows staged while
+//               the current one is transformed
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <math.h>
@@ -656,18 +657,20 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan 
 
 // The column stage as a persistent, software-pipelined kernel (the default;
 // k_cols_rc above is one CTA per tile).  A tile is (window, group of CP
-// columns); each CTA takes a contiguous range of tiles, so consecutive tiles
-// are the next column groups of the same window: the twiddles and the row
-// mask's spectrum are staged once per CTA and the patch means once per
-// window.  Per tile: the slave's mask rows (staged during the previous
-// tile's inverse transform) are transformed first, then the master's
-// (staged during the previous tile's copy-out and the slave transform); the
-// master's spectrum stays in registers for the product, after which the
-// slave slots are free and the next tile's slave rows are requested.  Rows
-// outside the slave's mask are zero in registers, never staged.  The
-// arithmetic is k_cols_rc's, operation for operation, so the results are the
-// same bits.  Tiles of column group 0 (the packed DC/Nyquist column, whose
-// second output goes through the slave slot) take k_cols_rc's order.
+// columns); CTAs take tiles a quarter window at a time from a counter, so a
+// CTA's consecutive tiles are mostly the next column groups of one window:
+// the twiddles and the row mask's spectrum are staged once per CTA and the
+// patch means once per run of a window's tiles.  Per tile: the slave's mask
+// rows (staged during the previous tile's inverse transform) are
+// transformed first, then the master's (staged during the previous tile's
+// copy-out and the slave transform); the master's spectrum stays in
+// registers for the product, after which the slave slots are free and the
+// next tile's slave rows are requested.  Rows outside the slave's mask are
+// zero in registers, never staged, and the slave's first FFT pass skips
+// their butterflies.  The arithmetic is k_cols_rc's, operation for
+// operation, so the results are the same bits.  Tiles of column group 0 (the
+// packed DC/Nyquist column, whose second output goes through the slave slot)
+// request the next tile's slave rows only after their copy-out.
 template <int M, int THR>
 __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan P) {
     using G = ColsGeom<M, THR>;

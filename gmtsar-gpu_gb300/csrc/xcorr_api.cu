@@ -4,7 +4,9 @@
 // The context replaces the reference's device plan and allocations
 // (d_allocate_arrays xcorr.cu:65-119, estimate_istep :161-230) and its strip
 // loop (do_correlation :299-378).  Windows run in batches sized to the
-// scratch; each batch is four kernel launches on one stream.
+// scratch, consecutive batches on two slots with their own streams; a batch
+// is the row stage (with shared row segments: the planner, then the rows),
+// the column stage, the peak stage and the subpixel stage.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
