@@ -360,7 +360,7 @@ xcg_status xcg_set_row_sharing(xcg_ctx *c, int32_t enable) {
 }
 
 xcg_status xcg_set_launch_shapes(xcg_ctx *c, int32_t cols_cfg, int32_t peak_cfg) {
-    if (!c || cols_cfg < 0 || cols_cfg > 2 || peak_cfg < 0 || peak_cfg > 1) return XCG_ERR_ARG;
+    if (!c || cols_cfg < 0 || cols_cfg > 2 || peak_cfg < 0 || peak_cfg > 2) return XCG_ERR_ARG;
     c->base.cols_cfg = cols_cfg;
     c->base.peak_cfg = peak_cfg;
     return XCG_OK;

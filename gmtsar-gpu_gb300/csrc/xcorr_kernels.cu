@@ -500,22 +500,28 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols(Plan P) 
 // the per-window host loop of d_do_freq_corr_strip (do_freq_xcorr.cu:150-195),
 // the time correlation d_calc_time_corr_strip (do_time_int_xcorr.cu:71-100),
 // d_scaled_strip (conv_ampl_demean.cu:50-68) and d_cppow_strip (:75-95).
-template <int N, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
+// row pairs of the largest surface (nyc = 512: windows of 512 rows)
+constexpr int PEAK_MAX_ROW_PAIRS = 256;
+
+template <int N, int MINB, int NT = 256>
+__global__ void __launch_bounds__(NT, MINB) k_peak(Plan P) {
     constexpr int T = fft_lanes(N);
     constexpr int PADN = fft_padded_len(N);
     constexpr int TWL = fft_twiddle_len(N);
     constexpr int PER = N / T;
-    constexpr int NT = 256;
+    constexpr int NW = NT / 32;
 
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     const int teams = NT / T;
     float2 *fb = tw + TWL;                                // [teams][PADN]
-    unsigned long long *rk = reinterpret_cast<unsigned long long *>(fb + teams * PADN);  // [8]
-    double *rd = reinterpret_cast<double *>(rk + 8);      // [2][8]
-    long long *ri64 = reinterpret_cast<long long *>(rd + 16);   // [3][8]
-    double *bc = reinterpret_cast<double *>(ri64 + 24);   // broadcast
+    unsigned long long *rk = reinterpret_cast<unsigned long long *>(fb + teams * PADN);  // [NW]
+    double *rd = reinterpret_cast<double *>(rk + NW);     // [2][NW]
+    long long *ri64 = reinterpret_cast<long long *>(rd + 2 * NW);   // [3][NW]
+    double *bc = reinterpret_cast<double *>(ri64 + 3 * NW);   // broadcast [4]
+    // [nyc / 2 <= 256] surface sum of each row pair, and its part in the reference's half blocks
+    float *rowf = reinterpret_cast<float *>(bc + 4);
+    float *rowh = rowf + PEAK_MAX_ROW_PAIRS;
 
     const int w = blockIdx.x;
     const int warp = threadIdx.x >> 5, l32 = threadIdx.x & 31;
@@ -574,7 +580,6 @@ __global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
     __syncthreads();
     const float keep = (float)bc[2];
     unsigned long long best = 0ull;
-    double hsum = 0.0, fsum = 0.0;
     const float2 *q = P.qspec + (size_t)w * nyc * P.qpitch;
     float *surf = P.surf + (size_t)w * nyc * nxc;
     for (int pr = team; pr < nyc / 2; pr += teams) {
@@ -590,9 +595,11 @@ __global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
             v[m] = (e <= N / 2) ? make_float2(q1.x - q2.y, q1.y + q2.x) : make_float2(q1.x + q2.y, q2.x - q1.y);
         }
         team_fft_reg<N, +1>(v, ex, tw, lane);
-        // surface sums: 16 values per lane and row pair in FP32, then double
-        // (GB300's FP64 pipe is a small fraction of its FP32 rate; the partial
-        // sums' rounding, ~1e-7 relative, is far below what the statistics need)
+        // surface sums: each row pair's in FP32 (the lane's values, then a
+        // fixed tree over the team), then the row pairs in double in a fixed
+        // order, so the sums do not depend on the launch shape (GB300's FP64
+        // pipe is a small fraction of its FP32 rate; the FP32 rounding, about
+        // 1e-7 relative, is far below what the statistics need)
         float fpart = 0.f, hpart = 0.f;
 #pragma unroll
         for (int m = 0; m < PER; m++) {
@@ -609,19 +616,26 @@ __global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
             if (!(e1 & 512u)) hpart += c1;      // reduce6<double,1024> keeps local [0,512) and [1024,1536)
             if (!(e2 & 512u)) hpart += c2;
         }
-        fsum += (double)fpart;
-        hsum += (double)hpart;
+#pragma unroll
+        for (int o = T / 2; o > 0; o >>= 1) {            // within the team
+            fpart += __shfl_xor_sync(0xffffffffu, fpart, o);
+            hpart += __shfl_xor_sync(0xffffffffu, hpart, o);
+        }
+        if (lane == 0) { rowf[pr] = fpart; rowh[pr] = hpart; }
     }
     best = warp_max_u64(best);
-    hsum = warp_sum_f64(hsum);
-    fsum = warp_sum_f64(fsum);
-    if (l32 == 0) { rk[warp] = best; rd[warp] = hsum; rd[8 + warp] = fsum; }
+    if (l32 == 0) rk[warp] = best;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long bb = rk[0];
-        double hs = rd[0], fs = rd[8];
-        for (int i = 1; i < NT / 32; i++) { bb = rk[i] > bb ? rk[i] : bb; hs += rd[i]; fs += rd[8 + i]; }
-        rk[0] = bb; rd[0] = hs; rd[8] = fs;
+    if (warp == 0) {
+        double hs = 0.0, fs = 0.0;
+        for (int i = l32; i < nyc / 2; i += 32) { hs += (double)rowh[i]; fs += (double)rowf[i]; }
+        hs = warp_sum_f64(hs);
+        fs = warp_sum_f64(fs);
+        if (l32 == 0) {
+            unsigned long long bb = rk[0];
+            for (int i = 1; i < NW; i++) bb = rk[i] > bb ? rk[i] : bb;
+            rk[0] = bb; rd[0] = hs; rd[NW] = fs;
+        }
     }
     __syncthreads();
     const unsigned pk = argmax_index(rk[0]);
@@ -668,11 +682,11 @@ __global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
         }
     }
     sn = warp_sum_i64(sn); s1 = warp_sum_i64(s1); s2 = warp_sum_i64(s2);
-    if (l32 == 0) { ri64[warp] = sn; ri64[8 + warp] = s1; ri64[16 + warp] = s2; }
+    if (l32 == 0) { ri64[warp] = sn; ri64[NW + warp] = s1; ri64[2 * NW + warp] = s2; }
     __syncthreads();
     if (threadIdx.x == 0) {
         long long tn = 0, t1 = 0, t2 = 0;
-        for (int i = 0; i < NT / 32; i++) { tn += ri64[i]; t1 += ri64[8 + i]; t2 += ri64[16 + i]; }
+        for (int i = 0; i < NW; i++) { tn += ri64[i]; t1 += ri64[NW + i]; t2 += ri64[2 * NW + i]; }
         const double gd = sqrt(1.0 * (double)t1 * (double)t2);
         const double gamma = (gd == 0.0) ? 0.0 : 100.0 * fabs((double)tn / gd);
         const double msc = cmax / gamma;
@@ -694,7 +708,7 @@ __global__ void __launch_bounds__(256, MINB) k_peak(Plan P) {
         o.cmax = cmax;
         const double inv_ns = pow2_inv(nxc * nyc);      // exact: nxc * nyc is a power of two
         o.cave = rd[0] * inv_ns;
-        o.cave_true = rd[8] * inv_ns;
+        o.cave_true = rd[NW] * inv_ns;
         o.gamma = gamma;
         o.mean1 = P.means[2 * w];
         o.mean2 = P.means[2 * w + 1];
@@ -944,13 +958,20 @@ static size_t cols_smem(int) {
 // resident k_peak CTAs per SM for configuration cfg
 template <int N>
 constexpr int peak_minb(int cfg) { return (N <= 256) ? (cfg == 1 ? 3 : 4) : (N <= 512 ? (cfg == 1 ? 2 : 3) : 1); }
-template <int N>
+template <int N, int NT = 256>
 static size_t peak_smem() {
     constexpr int T = fft_lanes(N);
-    const int teams = 256 / T;
+    constexpr int teams = NT / T, nw = NT / 32;
     return fft_twiddle_len(N) * sizeof(float2) + (size_t)teams * fft_padded_len(N) * sizeof(float2) +
-           8 * sizeof(unsigned long long) + 16 * sizeof(double) + 24 * sizeof(long long) + 4 * sizeof(double);
+           (size_t)nw * (sizeof(unsigned long long) + 2 * sizeof(double) + 3 * sizeof(long long)) + 4 * sizeof(double) +
+           (size_t)2 * PEAK_MAX_ROW_PAIRS * sizeof(float);
 }
+// launch shape 2: 512 threads per window (twice the teams per window, the
+// same warps per SM) for transforms up to 512 points
+template <int N>
+constexpr bool peak_wide_ok() { return N <= 512; }
+template <int N>
+constexpr int peak_wide_minb() { return N <= 256 ? 2 : 1; }
 static size_t subpix_smem(const Plan &P) {
     return 64 * sizeof(float) + (size_t)P.n2y * P.nx2 * sizeof(float2) + (size_t)P.ny2 * P.n2y * sizeof(float2) +
            (size_t)P.nx2 * P.n2x * sizeof(float2) + 8 * sizeof(unsigned long long) + 16;
@@ -983,6 +1004,10 @@ static cudaError_t setup_peak() {
     if (!e && peak_minb<N>(1) != peak_minb<N>(0))
         e = cudaFuncSetAttribute(k_peak<N, peak_minb<N>(1)>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)peak_smem<N>());
+    if constexpr (peak_wide_ok<N>())
+        if (!e)
+            e = cudaFuncSetAttribute(k_peak<N, peak_wide_minb<N>(), 512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)peak_smem<N, 512>());
     return e;
 }
 
@@ -1037,6 +1062,12 @@ static void launch_cols_t(const Plan &P, cudaStream_t s) {
 }
 template <int N>
 static void launch_peak_t(const Plan &P, cudaStream_t s) {
+    if constexpr (peak_wide_ok<N>()) {
+        if (P.peak_cfg == 2) {
+            k_peak<N, peak_wide_minb<N>(), 512><<<P.nwin, 512, peak_smem<N, 512>(), s>>>(P);
+            return;
+        }
+    }
     if (P.peak_cfg == 1) k_peak<N, peak_minb<N>(1)><<<P.nwin, 256, peak_smem<N>(), s>>>(P);
     else k_peak<N, peak_minb<N>(0)><<<P.nwin, 256, peak_smem<N>(), s>>>(P);
 }

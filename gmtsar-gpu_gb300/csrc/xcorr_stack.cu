@@ -102,7 +102,7 @@ static xcg_status get_bucket(xcg_stack *st, int xs, int ys, Bucket **out) {
                 if (n < 5 || a != 4 * xs || bb != 4 * ys || r != p.ri || i != p.interp_factor) continue;
                 b.batch = bt;
                 b.ctx->base.cols_cfg = (n >= 7 && cc >= 0 && cc <= 2) ? cc : 0;
-                b.ctx->base.peak_cfg = (n >= 7 && pc >= 0 && pc <= 1) ? pc : 0;
+                b.ctx->base.peak_cfg = (n >= 7 && pc >= 0 && pc <= 2) ? pc : 0;
                 b.ctx->base.rc = (n >= 8 && sh == 0) ? 0 : 1;
             }
             fclose(f);
@@ -388,11 +388,11 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
         }
         B.rc = best_share;
         B.cols_cfg = best_cols;
-        B.peak_cfg = 1;
-        {
+        for (int pc = 1; pc <= 2; pc++) {                 // the peak stage's residency, then 512 threads
+            B.peak_cfg = pc;
             float t;
             XCG_TRY(time_it(&t));
-            if (t < best) { best = t; best_peak = 1; }
+            if (t < best) { best = t; best_peak = pc; }
         }
         B.peak_cfg = best_peak;
         if (cache) {

@@ -199,7 +199,7 @@ typedef struct {
     int32_t bucket_cols_cfg[8];  /* column-stage launch shape (xcg_set_launch_shapes): with shared rows 0
                                     persistent, 1 one CTA per tile; without, 0 128-thread CTAs, two cp.async
                                     staging groups, 1 256-thread CTAs, 2 one staging group */
-    int32_t bucket_peak_cfg[8];  /* peak-stage residency: 0 four CTAs per SM, 1 three */
+    int32_t bucket_peak_cfg[8];  /* peak-stage launch shape (xcg_set_launch_shapes) */
     int32_t bucket_row_sharing[8];  /* 1: shared row segments, 0: one row stage per window */
 } xcg_stack_stats;
 
@@ -242,8 +242,10 @@ xcg_status xcg_set_row_sharing(xcg_ctx *ctx, int32_t enable);
  * 0 (default) persistent CTAs walking ranges of (window, column group)
  * tiles, the next tile's rows staged during the current one; 1 one CTA per
  * tile.  Without sharing: 0 128-thread CTAs, two cp.async staging groups;
- * 1 256-thread CTAs; 2 one staging group.  peak_cfg: 0 four CTAs per SM,
- * 1 three.  Every shape gives the same bits. */
+ * 1 256-thread CTAs; 2 one staging group.  peak_cfg: 0 four CTAs per SM of
+ * 256 threads per window (three for 512-point transforms), 1 one fewer,
+ * 2 512 threads per window (transforms up to 512 points; the others take
+ * 0).  Every shape gives the same bits. */
 xcg_status xcg_set_launch_shapes(xcg_ctx *ctx, int32_t cols_cfg, int32_t peak_cfg);
 
 /* Make later xcg_correlate_device calls on this context also write, per

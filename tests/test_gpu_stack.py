@@ -125,7 +125,7 @@ def test_autotune_and_split_strips(tmp_path, monkeypatch):
     lines = cache.read_text().splitlines()
     assert len(lines) >= 1 + 4 and all(len(l.split()) == 8 for l in lines[1:])
     s = st.stats()
-    assert all(0 <= s.bucket_cols_cfg[i] <= 2 and 0 <= s.bucket_peak_cfg[i] <= 1 for i in range(s.buckets))
+    assert all(0 <= s.bucket_cols_cfg[i] <= 2 and 0 <= s.bucket_peak_cfg[i] <= 2 for i in range(s.buckets))
     st.close()
 
 
@@ -163,12 +163,12 @@ def test_stack_every_bucket_against_oracle():
     st.close()
 
 
-@pytest.mark.parametrize("cols_cfg,peak_cfg", [(0, 1), (1, 0), (2, 1), (1, 1)])
+@pytest.mark.parametrize("cols_cfg,peak_cfg", [(0, 1), (1, 0), (2, 1), (1, 1), (0, 2), (2, 2)])
 def test_tuned_launch_shapes_give_identical_results(tmp_path, monkeypatch, cols_cfg, peak_cfg):
     """Every per-window launch shape the autotuner chooses between (256-thread
-    column CTAs, one cp.async staging group, three peak CTAs per SM) computes
-    the same transforms in the same order: results bit-identical to a
-    context with one row stage per window."""
+    column CTAs, one cp.async staging group, one peak CTA per SM fewer, 512
+    peak threads per window) computes the same transforms in the same order:
+    results bit-identical to a context with one row stage per window."""
     torch = pytest.importorskip("torch")
     items = _setup(torch)
     alone = []
