@@ -671,8 +671,11 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan 
 // operation, so the results are the same bits.  Tiles of column group 0 (the
 // packed DC/Nyquist column, whose second output goes through the slave slot)
 // request the next tile's slave rows only after their copy-out.
-template <int M, int THR>
-__global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan P) {
+// KEEP: the slave's column spectrum stays in registers for the product
+// (one CTA per SM fewer; the autotuner's column shape 2 with shared rows).
+template <int M, int THR, bool KEEP>
+__global__ void __launch_bounds__(THR, KEEP ? ColsGeom<M, THR>::BLOCKS - 1 : ColsGeom<M, THR>::BLOCKS)
+k_cols_rcp(Plan P) {
     using G = ColsGeom<M, THR>;
     constexpr int T = G::T, CS = G::CS, CP = G::CP, TWL = G::TWL;
     constexpr int PER = M / T;
@@ -799,8 +802,15 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
             z[m] = (m >= PER / 4 && m < 3 * PER / 4) ? pa[fft_pad(lane + T * m)] : make_float2(0.f, 0.f);
         __syncwarp();
         team_fft_reg_mid<M, -1>(z, pa, tw, lane);    // zero outside the mask rows
+        float2 zs[KEEP ? PER : 1];
+        if constexpr (KEEP) {
 #pragma unroll
-        for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
+            for (int m = 0; m < PER; m++) zs[m] = z[m];
+        }
+        if (!KEEP || b == 0) {                   // column group 0 splits the packed column from the slot
+#pragma unroll
+            for (int m = 0; m < PER; m++) pa[fft_pad(lane + T * m)] = z[m];
+        }
         cp_async_wait<0>();                      // master rows in
         __syncthreads();
 #pragma unroll
@@ -828,7 +838,8 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rcp(Plan
 #pragma unroll
             for (int m = 0; m < PER; m++) {
                 const int ky = lane + T * m;
-                z[m] = product(kx, z[m], pa[fft_pad(ky)], ky);
+                if constexpr (KEEP) z[m] = product(kx, z[m], zs[m], ky);
+                else z[m] = product(kx, z[m], pa[fft_pad(ky)], ky);
             }
         } else {
 #pragma unroll
@@ -930,7 +941,11 @@ static cudaError_t setup_cols_rc_t() {
     cudaError_t e = cudaFuncSetAttribute(k_cols_rc<M, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)cols_rc_smem<M>());
     if (e) return e;
-    return cudaFuncSetAttribute(k_cols_rcp<M, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cols_rc_smem<M>());
+    e = cudaFuncSetAttribute(k_cols_rcp<M, 128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)cols_rc_smem<M>());
+    if (e) return e;
+    return cudaFuncSetAttribute(k_cols_rcp<M, 128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)cols_rc_smem<M>());
 }
 
 cudaError_t segrows_setup(const Plan &P) {
@@ -1010,8 +1025,13 @@ static void launch_cols_rc_t(const Plan &P, cudaStream_t s) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (P.cols_cfg == 2 && G::BLOCKS > 1) {      // the slave spectrum kept in registers
+        const int grid = std::min(ntiles, sms * (G::BLOCKS - 1));
+        k_cols_rcp<M, 128, true><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
+        return;
+    }
     const int grid = std::min(ntiles, sms * G::BLOCKS);
-    k_cols_rcp<M, 128><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
+    k_cols_rcp<M, 128, false><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
 }
 void launch_cols_rc(const Plan &P, cudaStream_t s) {
     switch (P.npy) {

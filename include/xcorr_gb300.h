@@ -196,9 +196,7 @@ typedef struct {
     int64_t windows, launches, graph_replays, last_graph_launches;
     int32_t batches, last_graph_batches, buckets, pad;
     int32_t bucket_npx[8], bucket_npy[8], bucket_batch[8];
-    int32_t bucket_cols_cfg[8];  /* column-stage launch shape (xcg_set_launch_shapes): with shared rows 0
-                                    persistent, 1 one CTA per tile; without, 0 128-thread CTAs, two cp.async
-                                    staging groups, 1 256-thread CTAs, 2 one staging group */
+    int32_t bucket_cols_cfg[8];  /* column-stage launch shape (xcg_set_launch_shapes) */
     int32_t bucket_peak_cfg[8];  /* peak-stage launch shape (xcg_set_launch_shapes) */
     int32_t bucket_row_sharing[8];  /* 1: shared row segments, 0: one row stage per window */
 } xcg_stack_stats;
@@ -239,9 +237,10 @@ xcg_status xcg_set_row_sharing(xcg_ctx *ctx, int32_t enable);
 
 /* Launch shapes of this context's column and peak stages (the choices
  * xcg_stack_autotune makes per bucket).  cols_cfg with shared row segments:
- * 0 (default) persistent CTAs walking ranges of (window, column group)
- * tiles, the next tile's rows staged during the current one; 1 one CTA per
- * tile.  Without sharing: 0 128-thread CTAs, two cp.async staging groups;
+ * 0 (default) persistent CTAs taking (window, column group) tiles from a
+ * counter, the next tile's rows staged during the current one; 1 one CTA per
+ * tile; 2 persistent with the slave's column spectrum kept in registers (one
+ * CTA per SM fewer).  Without sharing: 0 128-thread CTAs, two cp.async staging groups;
  * 1 256-thread CTAs; 2 one staging group.  peak_cfg: 0 four CTAs per SM of
  * 256 threads per window (three for 512-point transforms), 1 one fewer,
  * 2 512 threads per window (transforms up to 512 points; the others take
