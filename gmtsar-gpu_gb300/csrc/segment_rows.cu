@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(THR, ColsGeom<M, THR>::BLOCKS) k_cols_rc(Plan 
 // packed DC/Nyquist column, whose second output goes through the slave slot)
 // request the next tile's slave rows only after their copy-out.
 // KEEP: the slave's column spectrum stays in registers for the product
-// (one CTA per SM fewer; the autotuner's column shape 2 with shared rows).
+// (one CTA per SM fewer; the default form up to 256-point columns).
 template <int M, int THR, bool KEEP>
 __global__ void __launch_bounds__(THR, KEEP ? ColsGeom<M, THR>::BLOCKS - 1 : ColsGeom<M, THR>::BLOCKS)
 k_cols_rcp(Plan P) {
@@ -1025,7 +1025,12 @@ static void launch_cols_rc_t(const Plan &P, cudaStream_t s) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (P.cols_cfg == 2 && G::BLOCKS > 1) {      // the slave spectrum kept in registers
+    // the slave spectrum kept in registers (one CTA per SM fewer): the
+    // default up to 256 points (0.454 against 0.481 ms per 1000 windows of
+    // 128 x 128), not beyond (full frame 72.4 against 69.5 ms); launch
+    // shape 2 takes the other form
+    const bool keep = (P.cols_cfg == 2) != (M <= 256);
+    if (keep && G::BLOCKS > 1) {
         const int grid = std::min(ntiles, sms * (G::BLOCKS - 1));
         k_cols_rcp<M, 128, true><<<grid, 128, cols_rc_smem<M>(), s>>>(P);
         return;

@@ -374,7 +374,7 @@ xcg_status xcg_stack_autotune(xcg_stack *st, const xcg_pair *pairs, int32_t npai
         b.batch = bestc;
         int best_cols = 0, best_peak = 0, best_share = 1;
         for (int cfg = 1; cfg <= 2; cfg++) {              // shared rows: one column-stage CTA per tile;
-            B.cols_cfg = cfg;                             // persistent with the slave spectrum in registers
+            B.cols_cfg = cfg;                             // the other persistent form
             float t;
             XCG_TRY(time_it(&t));
             if (t < best) { best = t; best_cols = cfg; }

@@ -238,9 +238,10 @@ xcg_status xcg_set_row_sharing(xcg_ctx *ctx, int32_t enable);
 /* Launch shapes of this context's column and peak stages (the choices
  * xcg_stack_autotune makes per bucket).  cols_cfg with shared row segments:
  * 0 (default) persistent CTAs taking (window, column group) tiles from a
- * counter, the next tile's rows staged during the current one; 1 one CTA per
- * tile; 2 persistent with the slave's column spectrum kept in registers (one
- * CTA per SM fewer).  Without sharing: 0 128-thread CTAs, two cp.async staging groups;
+ * counter, the next tile's rows staged during the current one, in the
+ * faster form for the size (up to 256-point columns the slave's column
+ * spectrum kept in registers at one CTA per SM fewer); 1 one CTA per tile;
+ * 2 persistent in the other form.  Without sharing: 0 128-thread CTAs, two cp.async staging groups;
  * 1 256-thread CTAs; 2 one staging group.  peak_cfg: 0 four CTAs per SM of
  * 256 threads per window (three for 512-point transforms), 1 one fewer,
  * 2 512 threads per window (transforms up to 512 points; the others take

@@ -105,7 +105,7 @@ def test_column_stage_forms_give_the_same_bits(xs, ys):
         per_tile = ctx.correlate(m, s, locs, 3, -4, 1e-3, strip_len=7)
         ctx.set_launch_shapes(0, 2)                  # and the peak stage at 512 threads per window
         wide_peak = ctx.correlate(m, s, locs, 3, -4, 1e-3, strip_len=7)
-        ctx.set_launch_shapes(2)                     # the slave spectrum kept in registers
+        ctx.set_launch_shapes(2)                     # the other persistent form (slave spectrum in registers or not)
         kept = ctx.correlate(m, s, locs, 3, -4, 1e-3, strip_len=7)
     assert persistent.tobytes() == per_tile.tobytes()
     assert wide_peak.tobytes() == per_tile.tobytes()
