@@ -158,7 +158,8 @@ xcg_status xcg_refiner_train_step(xcg_refiner *r, const float *d_feat, const flo
 // The plain path with the refiner standing in for the FFT interpolation
 // where it is confident (see k_decide); the other windows get the plain
 // subpixel result.  Per batch: rows, columns, peak (+ 9x9 neighbourhoods),
-// refiner inference, decision, subpixel for the rest.
+// refiner inference, decision, subpixel for the rest; the batches as
+// xcg_correlate_device runs them.
 xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *d_master, int32_t m_nx, int32_t m_ny,
                                         const void *d_slave, int32_t s_nx, int32_t s_ny,
                                         int32_t x_offset, int32_t y_offset, double astretcha,
@@ -170,6 +171,7 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *
     if (c->base.corr_mode != 2) { xcg::set_last_error("the refined path runs the frequency-domain mode only"); return XCG_ERR_UNSUPPORTED; }
     XCG_TRY(ck(cudaSetDevice(c->device), "cudaSetDevice"));
     memset(&c->stats, 0, sizeof c->stats);
+    c->stats.scratch_bytes = c->scratch_bytes;
     if (nlocs == 0) return XCG_OK;
     if (nlocs > c->ref_cap) {
         cudaFree(c->ref_feat); cudaFree(c->ref_pred); cudaFree(c->ref_skip);
@@ -179,8 +181,7 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *
         XCG_TRY(ck(cudaMalloc(&c->ref_skip, (size_t)nlocs), "cudaMalloc skip"));
         c->ref_cap = nlocs;
     }
-    int bw = c->max_batch;
-    if (strip_len > 0 && strip_len <= bw) bw = (bw / strip_len) * strip_len;
+    const int bw = xcg::ctx_batch_windows(c, nlocs, strip_len);
     xcg::Plan P = xcg::ctx_plan(c);
     P.single.master = d_master; P.single.m_nx = m_nx; P.single.m_ny = m_ny;
     P.single.slave = d_slave; P.single.s_nx = s_nx; P.single.s_ny = s_ny;
@@ -191,38 +192,30 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *
     P.single.feat = c->ref_feat;
     P.pairs = nullptr;
     P.winref = nullptr;
+    P.locs = d_locs;
+    P.skip = nullptr;
+    std::vector<int> starts;
+    for (int w = 0; w < nlocs; w += bw) starts.push_back(w);
+    starts.push_back(nlocs);
+    // the batches run through the plain path's scheduler (two scratch slots
+    // on their own streams, the planners ahead); each batch's subpixel launch
+    // becomes inference, decision and the subpixel stage for the windows the
+    // refiner left alone
+    auto tail = [&](const xcg::Plan &Q, cudaStream_t ss) -> xcg_status {
+        float *pred = c->ref_pred + (size_t)Q.win0 * 3;
+        xcg::ref_launch_infer(r->R, c->ref_feat + (size_t)Q.win0 * 81, pred, Q.nwin, ss);
+        xcg::launch_decide(Q, pred, c->ref_skip + Q.win0, max_sigma, max_disagree, ss);
+        xcg::Plan Qs = Q;
+        Qs.skip = c->ref_skip + Q.win0;
+        xcg::launch_subpix(Qs, ss);
+        c->stats.launches += 2;               // ctx_launch counts one
+        return XCG_OK;
+    };
     cudaStream_t s = (cudaStream_t)stream;
-    XCG_TRY(xcg::tc_reset_status(c, s));
-    for (int w0 = 0; w0 < nlocs; w0 += bw) {
-        P.win0 = w0;
-        P.nwin = (nlocs - w0 < bw) ? nlocs - w0 : bw;
-        P.locs = d_locs + w0;
-        P.skip = nullptr;
-        if (P.tc_form) {                         // precision form: tensor-core DFT stages
-            P.rc = 0;
-            xcg::launch_rows(P, s);
-            xcg::launch_tc_rows(P, s);
-            xcg::launch_tc_cols(P, s);
-            xcg::launch_tc_inv(P, s);
-            c->stats.launches += 2;
-        } else if (P.rc) {                       // shared row segments
-            xcg::launch_rc_plan(P, s);
-            xcg::launch_segrows(P, s);
-            xcg::launch_cols_rc(P, s);
-            c->stats.launches += 1;
-        } else {
-            xcg::launch_rows(P, s);
-            xcg::launch_cols(P, s);
-        }
-        xcg::launch_peak(P, s);
-        xcg::ref_launch_infer(r->R, c->ref_feat + (size_t)w0 * 81, c->ref_pred + (size_t)w0 * 3, P.nwin, s);
-        xcg::launch_decide(P, c->ref_pred + (size_t)w0 * 3, c->ref_skip + w0, max_sigma, max_disagree, s);
-        P.skip = c->ref_skip + w0;
-        xcg::launch_subpix(P, s);
-        c->stats.launches += 6;
-        c->stats.batches++;
-    }
-    c->stats.batch_windows = bw;
+    c->tl_tags.clear();
+    if (c->profiling == 2) XCG_TRY(xcg::tl_mark(c, s, 1));
+    XCG_TRY(xcg::ctx_launch(c, P, starts.data(), (int)starts.size() - 1, s, {}, tail));
+    if (c->profiling == 2) XCG_TRY(xcg::tl_finish(c, s));
     return ck(cudaGetLastError(), "refined path launch");
 }
 

@@ -495,7 +495,8 @@ int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len) {
     return bw;
 }
 
-xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s, const RowsHook &rows) {
+xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_t s, const RowsHook &rows,
+                      const RowsHook &tail) {
     // launch slots: rows, columns, peak, subpixel; the precision form splits
     // the column stage into three tensor-core DFT stages
     const bool tcf = P.tc_form != 0;
@@ -570,7 +571,10 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
                     case 2: launch_tc_cols(Q, ss); break;
                     case 3: launch_tc_inv(Q, ss); break;
                     case 4: launch_peak(Q, ss); break;
-                    case 5: launch_subpix(Q, ss); break;
+                    case 5:
+                        if (tail) { const xcg_status ts = tail(Q, ss); if (ts != XCG_OK) return ts; }
+                        else launch_subpix(Q, ss);
+                        break;
                 }
             } else {
                 switch (k) {
@@ -594,7 +598,10 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
                         else launch_cols(Q, ss);
                         break;
                     case 2: if (tm) launch_tpeak(Q, ss); else launch_peak(Q, ss); break;
-                    case 3: launch_subpix(Q, ss); break;
+                    case 3:
+                        if (tail) { const xcg_status ts = tail(Q, ss); if (ts != XCG_OK) return ts; }
+                        else launch_subpix(Q, ss);
+                        break;
                 }
             }
             if (c->profiling == 1) cudaEventRecord(c->events[ei++], ss);

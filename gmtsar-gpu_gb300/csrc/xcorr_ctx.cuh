@@ -68,8 +68,10 @@ Plan ctx_plan(const xcg_ctx *c);
 using RowsHook = std::function<xcg_status(const Plan &Q, cudaStream_t ss)>;
 // Launch the four kernels for windows [starts[b], starts[b+1]) of the
 // window arrays in P (locs, winref), b < nbatch; updates the context stats.
+// `tail`, when given, stands in for the subpixel launch of each batch (the
+// refined path: refiner inference, decision, subpixel stage for the rest).
 xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nbatch, cudaStream_t s,
-                      const RowsHook &rows = {});
+                      const RowsHook &rows = {}, const RowsHook &tail = {});
 // Timeline mode: record mark `tag` on stream ss; tl_finish (after the call's
 // work was enqueued) waits for the device and fills the stats' timeline.
 xcg_status tl_mark(xcg_ctx *c, cudaStream_t ss, int tag);
