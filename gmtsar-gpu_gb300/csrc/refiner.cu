@@ -373,8 +373,30 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 // 288 -> 64 layer as tensor-core tiles with bias + GELU applied to the
 // accumulators, the 64 -> 3 layer as warp dot products.  With the
 // activations channel-last, each A-fragment element pair is one 32-bit load.
+// the decision of RefDecide for window w: r3 = (fx, fy, s), f its 9x9 neighbourhood
+__device__ static void ref_decide(const RefDecide &D, int w, const float *r3, const float *f) {
+    const float fx = r3[0], fy = r3[1], sg = expf(0.5f * r3[2]);
+    auto vertex = [](float a, float b, float c) {
+        const float den = a - 2.f * b + c;
+        return (den < 0.f) ? 0.5f * (a - c) / den : 0.f;
+    };
+    const float px = vertex(f[4 * 9 + 3], f[4 * 9 + 4], f[4 * 9 + 5]);
+    const float py = vertex(f[3 * 9 + 4], f[4 * 9 + 4], f[5 * 9 + 4]);
+    const bool ok = (sg < D.max_sigma) && fabsf(fx - px) < D.max_dis && fabsf(fy - py) < D.max_dis &&
+                    isfinite(fx) && isfinite(fy) && f[4 * 9 + 4] > 0.f;
+    D.skip[w] = ok ? 1 : 0;
+    if (ok) {
+        xcg_result &o = D.res[w];
+        o.xfrac = fx;
+        o.yfrac = fy;
+        o.fip = -1;
+        o.fjp = -1;
+        o.flags |= XCG_FLAG_REFINED;
+    }
+}
+
 __global__ void __launch_bounds__(128 * INF_GROUPS) k_ref_infer(RefPlan R, const float *__restrict__ feat,
-                                                                 float *__restrict__ out, int n) {
+                                                                 float *__restrict__ out, int n, RefDecide D) {
     extern __shared__ __align__(16) unsigned char smc[];
     const __nv_bfloat16 *B2 = reinterpret_cast<const __nv_bfloat16 *>(smc);    // [32][INF_KS]
     const __nv_bfloat16 *B3 = B2 + 32 * INF_KS;
@@ -466,15 +488,18 @@ __global__ void __launch_bounds__(128 * INF_GROUPS) k_ref_infer(RefPlan R, const
                     }
         }
         __syncthreads();
-        // 64 -> 3
+        // 64 -> 3, then the decision (x0 still holds the neighbourhood)
         if (warp == 0 && have) {
+            float r3[3];
 #pragma unroll
             for (int o = 0; o < 3; o++) {
                 float v = fmaf(F2[o * 64 + lane], g1[lane], F2[o * 64 + 32 + lane] * g1[32 + lane]);
 #pragma unroll
                 for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-                if (lane == 0) out[(size_t)w * 3 + o] = v + c2[o];
+                r3[o] = v + c2[o];
+                if (lane == 0) out[(size_t)w * 3 + o] = r3[o];
             }
+            if (D.skip && lane == 0) ref_decide(D, w, r3, x0);
         }
         __syncthreads();                           // x0 .. g1 are reused by the next window
     }
@@ -508,11 +533,12 @@ void ref_launch_adam(const RefPlan &R, float lr, int step, cudaStream_t s) {
     k_ref_adam<<<(RP_N + 255) / 256, 256, 0, s>>>(R, lr, b1, b2, 1e-8f, c1, c2);
 }
 void ref_launch_derive(const RefPlan &R, cudaStream_t s) { k_ref_derive<<<(RP_N + 255) / 256, 256, 0, s>>>(R); }
-void ref_launch_infer(const RefPlan &R, const float *feat, float *out, int n, cudaStream_t s) {
+void ref_launch_infer(const RefPlan &R, const float *feat, float *out, int n, cudaStream_t s, const RefDecide *D) {
     // INF_GROUPS windows per CTA at a time, two CTAs per SM (91 KB of shared memory each)
     const int need = (n + INF_GROUPS - 1) / INF_GROUPS;
     const int blocks = need < 2 * 152 ? need : 2 * 152;
-    k_ref_infer<<<blocks > 0 ? blocks : 1, 128 * INF_GROUPS, ref_infer_smem(), s>>>(R, feat, out, n);
+    const RefDecide none{nullptr, nullptr, 0.f, 0.f};
+    k_ref_infer<<<blocks > 0 ? blocks : 1, 128 * INF_GROUPS, ref_infer_smem(), s>>>(R, feat, out, n, D ? *D : none);
 }
 
 }  // namespace xcg

@@ -3,6 +3,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "xcorr_gb300.h"
+
 namespace xcg {
 
 // flat parameter vector (FP32): conv weights [c_out][c_in][3][3], dense [out][in]
@@ -37,6 +39,18 @@ void ref_launch_bwd(const RefPlan &R, const float *target, int n, cudaStream_t s
 void ref_launch_wgrad(const RefPlan &R, const float *feat, int n, cudaStream_t s);
 void ref_launch_adam(const RefPlan &R, float lr, int step, cudaStream_t s);
 void ref_launch_derive(const RefPlan &R, cudaStream_t s);
-void ref_launch_infer(const RefPlan &R, const float *feat, float *out, int n, cudaStream_t s);
+// The refined path's decision, taken by the inference kernel for each window
+// it evaluates: the refiner's (fx, fy) replace the FFT interpolation where
+// the predicted standard deviation exp(s/2) is below max_sigma and both
+// coordinates lie within max_dis of a three-point parabola fit through the
+// centre row and column of the 9x9 neighbourhood.
+struct RefDecide {
+    xcg_result *res;              // [n] the windows' result records
+    unsigned char *skip;          // [n] 1: refined, the subpixel stage leaves the window alone
+    float max_sigma, max_dis;
+};
+// Inference of n windows' (fx, fy, s); with D, also the decision above.
+void ref_launch_infer(const RefPlan &R, const float *feat, float *out, int n, cudaStream_t s,
+                      const RefDecide *D = nullptr);
 
 }  // namespace xcg

@@ -156,7 +156,7 @@ xcg_status xcg_refiner_train_step(xcg_refiner *r, const float *d_feat, const flo
 }
 
 // The plain path with the refiner standing in for the FFT interpolation
-// where it is confident (see k_decide); the other windows get the plain
+// where it is confident (see RefDecide); the other windows get the plain
 // subpixel result.  Per batch: rows, columns, peak (+ 9x9 neighbourhoods),
 // refiner inference, decision, subpixel for the rest; the batches as
 // xcg_correlate_device runs them.
@@ -199,16 +199,15 @@ xcg_status xcg_correlate_device_refined(xcg_ctx *c, xcg_refiner *r, const void *
     starts.push_back(nlocs);
     // the batches run through the plain path's scheduler (two scratch slots
     // on their own streams, the planners ahead); each batch's subpixel launch
-    // becomes inference, decision and the subpixel stage for the windows the
-    // refiner left alone
+    // becomes inference with the decision, and the subpixel stage for the
+    // windows the refiner left alone
     auto tail = [&](const xcg::Plan &Q, cudaStream_t ss) -> xcg_status {
-        float *pred = c->ref_pred + (size_t)Q.win0 * 3;
-        xcg::ref_launch_infer(r->R, c->ref_feat + (size_t)Q.win0 * 81, pred, Q.nwin, ss);
-        xcg::launch_decide(Q, pred, c->ref_skip + Q.win0, max_sigma, max_disagree, ss);
+        const xcg::RefDecide D{d_results + Q.win0, c->ref_skip + Q.win0, max_sigma, max_disagree};
+        xcg::ref_launch_infer(r->R, c->ref_feat + (size_t)Q.win0 * 81, c->ref_pred + (size_t)Q.win0 * 3, Q.nwin, ss, &D);
         xcg::Plan Qs = Q;
         Qs.skip = c->ref_skip + Q.win0;
         xcg::launch_subpix(Qs, ss);
-        c->stats.launches += 2;               // ctx_launch counts one
+        c->stats.launches += 1;               // ctx_launch counts one
         return XCG_OK;
     };
     cudaStream_t s = (cudaStream_t)stream;

@@ -876,44 +876,6 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
     }
 }
 
-// ---------------------------------------------------------------- k_decide
-// Takes the refiner's (fx, fy, s) for each window of the batch when it is
-// confident: predicted standard deviation exp(s/2) below max_sigma and both
-// coordinates within max_dis of a three-point parabola fit of the 9x9
-// neighbourhood; those windows get xfrac = fx, yfrac = fy (surface pixels,
-// as highres_corr.cu:67-76 defines them) and XCG_FLAG_REFINED, and are
-// skipped by k_subpix.
-__global__ void k_decide(Plan P, const float *__restrict__ pred, unsigned char *skip, float max_sigma, float max_dis) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= P.nwin) return;
-    int local, pidx;
-    const PairDev pd = pair_of(P, w, local, pidx);
-    const float *f = pd.feat + (size_t)local * 81;
-    const float fx = pred[3 * w], fy = pred[3 * w + 1], sg = expf(0.5f * pred[3 * w + 2]);
-    auto vertex = [](float a, float b, float c) {
-        const float den = a - 2.f * b + c;
-        return (den < 0.f) ? 0.5f * (a - c) / den : 0.f;
-    };
-    const float px = vertex(f[4 * 9 + 3], f[4 * 9 + 4], f[4 * 9 + 5]);
-    const float py = vertex(f[3 * 9 + 4], f[4 * 9 + 4], f[5 * 9 + 4]);
-    const bool ok = (sg < max_sigma) && fabsf(fx - px) < max_dis && fabsf(fy - py) < max_dis &&
-                    isfinite(fx) && isfinite(fy) && f[4 * 9 + 4] > 0.f;
-    skip[w] = ok ? 1 : 0;
-    if (ok) {
-        xcg_result &o = pd.out[local];
-        o.xfrac = fx;
-        o.yfrac = fy;
-        o.fip = -1;
-        o.fjp = -1;
-        o.flags |= XCG_FLAG_REFINED;
-    }
-}
-
-void launch_decide(const Plan &P, const float *pred, unsigned char *skip, float max_sigma, float max_dis,
-                   cudaStream_t s) {
-    k_decide<<<(P.nwin + 127) / 128, 128, 0, s>>>(P, pred, skip, max_sigma, max_dis);
-}
-
 // ---------------------------------------------------------------- launchers
 
 int put_row_phase(float2 *dst, int n, int ri) {

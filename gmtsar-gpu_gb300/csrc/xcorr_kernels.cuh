@@ -10,8 +10,6 @@ void launch_rows(const Plan &P, cudaStream_t s);
 void launch_cols(const Plan &P, cudaStream_t s);
 void launch_peak(const Plan &P, cudaStream_t s);
 void launch_subpix(const Plan &P, cudaStream_t s);
-void launch_decide(const Plan &P, const float *pred, unsigned char *skip, float max_sigma, float max_dis,
-                   cudaStream_t s);
 void set_last_error(const char *msg);
 // Range-interpolation table of the row kernel for n-point rows and factor ri
 // (Plan::phase), written to dst; returns the entries written, (ri-1)*n (1
