@@ -271,44 +271,55 @@ xcg_status xcg_create(const xcg_params *p, int32_t device, int32_t max_batch, xc
         if ((size_t)mb * pw * c->nslots > budget) mb = (int)(budget / (pw * c->nslots));
         if (mb < 1) { st = XCG_ERR_NOMEM; g_last_error = "not enough device memory for one window"; goto fail; }
         c->max_batch = mb;
-        size_t off = 0;
-        auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes * (size_t)mb); return o; };
-        c->off_means = take(2 * sizeof(double));
-        c->off_qspec = take((size_t)B.nyc * B.qpitch * sizeof(float2));
-        c->off_surf = take((size_t)B.nyc * B.nxc * sizeof(float));
-        c->off_md = take(64 * sizeof(float));
-        c->off_mdnext = take(64);
-        c->off_corr0n = take(sizeof(double));
-        // the two row-stage layouts share one region: one row stage per
-        // window (per-window arrays), or shared row segments (chunk arrays);
-        // a batch uses one of them, and a slot's next batch starts after it
-        const size_t region = off;
-        c->off_zrow = take((size_t)B.npy * B.npx * sizeof(float2));
-        c->off_amp1 = take((size_t)B.npy * B.npx * sizeof(float));
-        c->off_amp2c = take((size_t)B.ny_corr * B.nx_corr * sizeof(float));
-        c->off_part = take((size_t)2 * B.nchunks * sizeof(float));
-        c->off_oob = take((size_t)B.nchunks);
-        c->off_minmax = take((size_t)4 * B.nchunks * sizeof(float));
-        const size_t end_pw = off;
-        off = region;
-        const size_t ch = (size_t)2 * B.nchunks;        // chunks per window at most
-        c->off_rc_desc = take(ch * sizeof(int4));
-        c->off_rc_wch = take(sizeof(int2));
-        c->off_rc_count = take(sizeof(int));
-        c->off_rc_amp = take(ch * 1024 * sizeof(float));
-        c->off_rc_spec = take(ch * 512 * sizeof(float2));
-        c->off_rc_part = take(ch * sizeof(float));
-        c->off_rc_minmax = take(ch * sizeof(float2));
-        c->off_rc_oob = take(ch);
-        c->off_rc_order = take(ch * sizeof(int));
-        c->off_rc_band_start = take(sizeof(int));       // 9 ints: one 256-byte block at least
-        c->off_rc_tile_next = take(sizeof(int));
-        if (off < end_pw) off = end_pw;
-        c->slot_bytes = align256(off);
-        c->scratch_bytes = c->slot_bytes * (size_t)c->nslots;
+        // one slot's arrays for mbw windows
+        auto layout = [&](int mbw) {
+            xcg_ctx::Layout L{};
+            L.windows = mbw;
+            size_t off = 0;
+            auto take = [&](size_t bytes) { size_t o = off; off += align256(bytes * (size_t)mbw); return o; };
+            L.means = take(2 * sizeof(double));
+            L.qspec = take((size_t)B.nyc * B.qpitch * sizeof(float2));
+            L.surf = take((size_t)B.nyc * B.nxc * sizeof(float));
+            L.md = take(64 * sizeof(float));
+            L.mdnext = take(64);
+            L.corr0n = take(sizeof(double));
+            // the two row-stage layouts share one region: one row stage per
+            // window (per-window arrays), or shared row segments (chunk arrays);
+            // a batch uses one of them, and a slot's next batch starts after it
+            const size_t region = off;
+            L.zrow = take((size_t)B.npy * B.npx * sizeof(float2));
+            L.amp1 = take((size_t)B.npy * B.npx * sizeof(float));
+            L.amp2c = take((size_t)B.ny_corr * B.nx_corr * sizeof(float));
+            L.part = take((size_t)2 * B.nchunks * sizeof(float));
+            L.oob = take((size_t)B.nchunks);
+            L.minmax = take((size_t)4 * B.nchunks * sizeof(float));
+            const size_t end_pw = off;
+            off = region;
+            const size_t ch = (size_t)2 * B.nchunks;        // chunks per window at most
+            L.rc_desc = take(ch * sizeof(int4));
+            L.rc_wch = take(sizeof(int2));
+            L.rc_count = take(sizeof(int));
+            L.rc_amp = take(ch * 1024 * sizeof(float));
+            L.rc_spec = take(ch * 512 * sizeof(float2));
+            L.rc_part = take(ch * sizeof(float));
+            L.rc_minmax = take(ch * sizeof(float2));
+            L.rc_oob = take(ch);
+            L.rc_order = take(ch * sizeof(int));
+            L.rc_band_start = take(sizeof(int));       // 9 ints: one 256-byte block at least
+            L.rc_tile_next = take(sizeof(int));
+            if (off < end_pw) off = end_pw;
+            L.slot_bytes = align256(off);
+            return L;
+        };
+        c->lay[0] = layout(mb);
+        c->scratch_bytes = c->lay[0].slot_bytes * (size_t)c->nslots;
+        if (mb >= 2) {                 // half slots: the same memory, give or take the alignment
+            c->lay[1] = layout(mb / 2);
+            c->scratch_bytes = std::max(c->scratch_bytes, c->lay[1].slot_bytes * (size_t)(2 * c->nslots));
+        }
         XCG_CK_C(cudaMalloc(&c->d_scratch, c->scratch_bytes), "cudaMalloc scratch");
         XCG_CK_C(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        for (int k = 0; k < c->nslots; k++) {
+        for (int k = 0; k < xcg_ctx::MAX_LANES; k++) {
             XCG_CK_C(cudaStreamCreateWithFlags(&c->slot_stream[k], cudaStreamNonBlocking), "cudaStreamCreate");
             XCG_CK_C(cudaEventCreateWithFlags(&c->ev_join[k], cudaEventDisableTiming), "cudaEventCreate");
         }
@@ -341,7 +352,7 @@ void xcg_destroy(xcg_ctx *c) {
     cudaFree(c->tc_prep);
     cudaFree(c->tc_err);
     for (cudaEvent_t ev : c->events) cudaEventDestroy(ev);
-    for (int k = 0; k < 2; k++) {
+    for (int k = 0; k < xcg_ctx::MAX_LANES; k++) {
         if (c->slot_stream[k]) { cudaStreamSynchronize(c->slot_stream[k]); cudaStreamDestroy(c->slot_stream[k]); }
         if (c->ev_join[k]) cudaEventDestroy(c->ev_join[k]);
     }
@@ -351,6 +362,12 @@ void xcg_destroy(xcg_ctx *c) {
     for (cudaEvent_t ev : c->tl_events) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+xcg_status xcg_set_batches(xcg_ctx *c, int32_t batches) {
+    if (!c || batches < 0) return XCG_ERR_ARG;
+    c->batches_cfg = batches;
+    return XCG_OK;
 }
 
 xcg_status xcg_set_row_sharing(xcg_ctx *c, int32_t enable) {
@@ -415,47 +432,36 @@ xcg_status xcg_correlate_device(xcg_ctx *c, const void *d_master, int32_t m_nx, 
 
 namespace xcg {
 
-Plan ctx_plan(const xcg_ctx *c) {
-    Plan P = c->base;
-    char *sc = (char *)c->d_scratch;
-    P.zrow = (float2 *)(sc + c->off_zrow);
-    P.amp1 = (float *)(sc + c->off_amp1);
-    P.amp2c = (float *)(sc + c->off_amp2c);
-    P.part = (float *)(sc + c->off_part);
-    P.oobmap = (unsigned char *)(sc + c->off_oob);
-    P.minmax = (float *)(sc + c->off_minmax);
-    P.means = (double *)(sc + c->off_means);
-    P.qspec = (float2 *)(sc + c->off_qspec);
-    P.surf = (float *)(sc + c->off_surf);
-    P.md = (float *)(sc + c->off_md);
-    P.mdnext = (unsigned char *)(sc + c->off_mdnext);
-    P.corr0n = (double *)(sc + c->off_corr0n);
-    P.rc_desc = (int4 *)(sc + c->off_rc_desc);
-    P.rc_wch = (int2 *)(sc + c->off_rc_wch);
-    P.rc_count = (int *)(sc + c->off_rc_count);
-    P.rc_amp = (float *)(sc + c->off_rc_amp);
-    P.rc_spec = (float2 *)(sc + c->off_rc_spec);
-    P.rc_part = (float *)(sc + c->off_rc_part);
-    P.rc_minmax = (float2 *)(sc + c->off_rc_minmax);
-    P.rc_oob = (unsigned char *)(sc + c->off_rc_oob);
-    P.rc_order = (int *)(sc + c->off_rc_order);
-    P.rc_band_start = (int *)(sc + c->off_rc_band_start);
-    P.rc_tile_next = (int *)(sc + c->off_rc_tile_next);
+Plan in_lane(const xcg_ctx *c, Plan P, int mode, int lane) {
+    const xcg_ctx::Layout &L = c->lay[mode];
+    char *sc = (char *)c->d_scratch + (size_t)lane * L.slot_bytes;
+    P.zrow = (float2 *)(sc + L.zrow);
+    P.amp1 = (float *)(sc + L.amp1);
+    P.amp2c = (float *)(sc + L.amp2c);
+    P.part = (float *)(sc + L.part);
+    P.oobmap = (unsigned char *)(sc + L.oob);
+    P.minmax = (float *)(sc + L.minmax);
+    P.means = (double *)(sc + L.means);
+    P.qspec = (float2 *)(sc + L.qspec);
+    P.surf = (float *)(sc + L.surf);
+    P.md = (float *)(sc + L.md);
+    P.mdnext = (unsigned char *)(sc + L.mdnext);
+    P.corr0n = (double *)(sc + L.corr0n);
+    P.rc_desc = (int4 *)(sc + L.rc_desc);
+    P.rc_wch = (int2 *)(sc + L.rc_wch);
+    P.rc_count = (int *)(sc + L.rc_count);
+    P.rc_amp = (float *)(sc + L.rc_amp);
+    P.rc_spec = (float2 *)(sc + L.rc_spec);
+    P.rc_part = (float *)(sc + L.rc_part);
+    P.rc_minmax = (float2 *)(sc + L.rc_minmax);
+    P.rc_oob = (unsigned char *)(sc + L.rc_oob);
+    P.rc_order = (int *)(sc + L.rc_order);
+    P.rc_band_start = (int *)(sc + L.rc_band_start);
+    P.rc_tile_next = (int *)(sc + L.rc_tile_next);
     return P;
 }
 
-// The plan with every scratch pointer moved by off bytes (another slot).
-static Plan with_slot(Plan P, size_t off) {
-    if (!off) return P;
-    auto mv = [off](auto *p) { return reinterpret_cast<decltype(p)>(reinterpret_cast<char *>(p) + off); };
-    P.zrow = mv(P.zrow); P.amp1 = mv(P.amp1); P.amp2c = mv(P.amp2c); P.part = mv(P.part);
-    P.oobmap = mv(P.oobmap); P.minmax = mv(P.minmax); P.means = mv(P.means); P.qspec = mv(P.qspec);
-    P.surf = mv(P.surf); P.md = mv(P.md); P.mdnext = mv(P.mdnext); P.corr0n = mv(P.corr0n);
-    P.rc_desc = mv(P.rc_desc); P.rc_wch = mv(P.rc_wch); P.rc_count = mv(P.rc_count); P.rc_amp = mv(P.rc_amp);
-    P.rc_spec = mv(P.rc_spec); P.rc_part = mv(P.rc_part); P.rc_minmax = mv(P.rc_minmax); P.rc_oob = mv(P.rc_oob);
-    P.rc_order = mv(P.rc_order); P.rc_band_start = mv(P.rc_band_start); P.rc_tile_next = mv(P.rc_tile_next);
-    return P;
-}
+Plan ctx_plan(const xcg_ctx *c) { return in_lane(c, c->base, 0, 0); }
 
 // Windows [off, off + n) of batch plan P as a plan of their own, for the row
 // stage, whose kernel writes only the per-window arrays below.
@@ -489,6 +495,7 @@ int ctx_batch_windows(const xcg_ctx *c, int nlocs, int strip_len) {
     // shows the device busy from the end of the first batch's row stage on.
     int bw = c->max_batch;
     if ((c->base.tc_form || c->base.rc) && nlocs >= 512 && (nlocs + 1) / 2 < bw) bw = (nlocs + 1) / 2;
+    if (c->batches_cfg > 0) bw = std::min(c->max_batch, (nlocs + c->batches_cfg - 1) / c->batches_cfg);
     if (strip_len > 0 && strip_len <= bw) bw = ((bw + strip_len - 1) / strip_len) * strip_len;   // whole strips
     if (bw > c->max_batch) bw = (c->max_batch / (strip_len > 0 ? strip_len : 1)) * (strip_len > 0 ? strip_len : 1);
     if (bw < 1) bw = c->max_batch;
@@ -520,28 +527,35 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
     // batches alternate between the scratch slots on the slot streams (forked
     // from and joined back into s); profiling runs them in order on s so each
     // kernel's events time that kernel alone
-    const bool fork = nb > 1 && c->nslots > 1 && c->profiling != 1;
-    const bool tl = c->profiling == 2;
-    for (int b = 0; b < nb; b++)           // before anything is enqueued
+    int widest = 0;
+    for (int b = 0; b < nb; b++) {         // before anything is enqueued
         if (starts[b + 1] - starts[b] > c->max_batch) {
             set_last_error("batch larger than the context's scratch");
             return XCG_ERR_TOO_LARGE;
         }
+        widest = std::max(widest, starts[b + 1] - starts[b]);
+    }
+    // more batches than slots, each fitting in half a slot: they run in the
+    // half-slot lanes, four in flight instead of two
+    const int mode = (nb > c->nslots && c->lay[1].windows > 0 && widest <= c->lay[1].windows) ? 1 : 0;
+    const int lanes = mode ? 2 * c->nslots : c->nslots;
+    const bool fork = nb > 1 && lanes > 1 && c->profiling != 1;
+    const bool tl = c->profiling == 2;
     if (tcf) {             // a timeout of an earlier call must not be reported by this one
         const xcg_status rs = tc_reset_status(c, s);
         if (rs != XCG_OK) return rs;
     }
     if (fork) {
         XCG_CK(cudaEventRecord(c->ev_fork, s), "cudaEventRecord");
-        for (int k = 0; k < c->nslots; k++) XCG_CK(cudaStreamWaitEvent(c->slot_stream[k], c->ev_fork, 0), "cudaStreamWaitEvent");
+        for (int k = 0; k < lanes; k++) XCG_CK(cudaStreamWaitEvent(c->slot_stream[k], c->ev_fork, 0), "cudaStreamWaitEvent");
     }
     // shared row segments through the device entry: the first batches'
     // planners (one CTA each, reading only the locations) go first on their
     // slot streams, so a later batch's plan is ready when its rows start
     // instead of waiting for an SM behind the earlier batch's row stage
-    const int npre = (rc && fork && !rows) ? std::min(nb, c->nslots) : 0;
+    const int npre = (rc && fork && !rows) ? std::min(nb, lanes) : 0;
     for (int b = 0; b < npre; b++) {
-        Plan Q = with_slot(P, (size_t)b * c->slot_bytes);
+        Plan Q = in_lane(c, P, mode, b);
         Q.win0 = starts[b];
         Q.nwin = starts[b + 1] - starts[b];
         Q.locs = locs0 + Q.win0;
@@ -549,9 +563,9 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
         launch_rc_plan(Q, c->slot_stream[b]);
     }
     for (int b = 0; b < nb; b++) {
-        const int slot = fork ? b % c->nslots : 0;
-        cudaStream_t ss = fork ? c->slot_stream[slot] : s;
-        Plan Q = with_slot(P, (size_t)slot * c->slot_bytes);
+        const int lane = fork ? b % lanes : 0;
+        cudaStream_t ss = fork ? c->slot_stream[lane] : s;
+        Plan Q = in_lane(c, P, mode, lane);
         Q.win0 = starts[b];
         Q.nwin = starts[b + 1] - starts[b];
         if (Q.nwin > c->max_batch) { set_last_error("batch larger than the context's scratch"); return XCG_ERR_TOO_LARGE; }
@@ -616,7 +630,7 @@ xcg_status ctx_launch(xcg_ctx *c, Plan P, const int *starts, int nb, cudaStream_
         }
     }
     if (fork) {
-        for (int k = 0; k < c->nslots; k++) {
+        for (int k = 0; k < lanes; k++) {
             XCG_CK(cudaEventRecord(c->ev_join[k], c->slot_stream[k]), "cudaEventRecord");
             XCG_CK(cudaStreamWaitEvent(s, c->ev_join[k], 0), "cudaStreamWaitEvent");
         }
@@ -722,7 +736,17 @@ xcg_status xcg_correlate(xcg_ctx *c, const void *master, int32_t m_nx, int32_t m
     // only the first band's copy is exposed; later bands copy while earlier
     // rows are transformed (a band copies in about half the time its rows'
     // kernels take).  Rows no window reads are not copied.
-    const int bw = xcg::ctx_batch_windows(c, nlocs, strip_len);
+    // Four batches of whole strips in the half-slot lanes when they fit
+    // (shared row segments): the first batch's column and peak stages start
+    // while later bands are still copying.  0.640 against 0.654 ms per call
+    // on 1000 windows of 128 x 128 (two batches); on the device entry, with
+    // the images resident, two batches are faster (0.461 against 0.499 ms).
+    int bw = xcg::ctx_batch_windows(c, nlocs, strip_len);
+    if (c->batches_cfg == 0 && c->base.rc && !c->base.tc_form && c->base.corr_mode == 2 && nlocs >= 800) {
+        int q = (nlocs + 3) / 4;
+        if (strip_len > 0) q = ((q + strip_len - 1) / strip_len) * strip_len;
+        if (q <= c->lay[1].windows) bw = q;
+    }
     std::vector<int> bounds;
     for (int w = 0; w < nlocs; w += bw) bounds.push_back(w);
     bounds.push_back(nlocs);

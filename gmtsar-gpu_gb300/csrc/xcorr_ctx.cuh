@@ -17,22 +17,32 @@ struct xcg_ctx {
     // scratch
     void *d_scratch = nullptr;
     size_t scratch_bytes = 0;     // all slots
-    size_t slot_bytes = 0;        // one slot: scratch for max_batch windows
     int max_batch = 0;            // windows per batch (per slot)
     // consecutive batches alternate between slots on their own streams, so
-    // one batch's column/peak stages overlap the next batch's row stage
+    // one batch's column/peak stages overlap the next batch's row stage; a
+    // call whose batches fit in half a slot runs them in 2 nslots lanes, each
+    // half of a slot, so that four batches are in flight
     int nslots = 2;
-    cudaStream_t slot_stream[2] = {nullptr, nullptr};
-    cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+    static constexpr int MAX_LANES = 4;
+    cudaStream_t slot_stream[MAX_LANES] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[MAX_LANES] = {};
+    int batches_cfg = 0;          // xcg_set_batches: batches per call (0: automatic)
     // host entry: the two images are copied on one stream in row bands, and
     // each row-stage sub-launch waits only for its band
     cudaStream_t copy_stream = nullptr;
     std::vector<cudaEvent_t> band_ready;      // one per band of a call
-    size_t off_zrow, off_amp1, off_amp2c, off_part, off_oob, off_minmax, off_means, off_qspec, off_surf, off_md,
-        off_mdnext, off_corr0n;
-    // shared row segments (segment_rows.cu): chunk arrays per slot
-    size_t off_rc_desc, off_rc_wch, off_rc_count, off_rc_amp, off_rc_spec, off_rc_part, off_rc_minmax, off_rc_oob,
-        off_rc_order, off_rc_band_start, off_rc_tile_next;
+    // scratch arrays of one slot (offsets from its start) for a batch capacity
+    struct Layout {
+        size_t zrow, amp1, amp2c, part, oob, minmax, means, qspec, surf, md, mdnext, corr0n;
+        // shared row segments (segment_rows.cu): chunk arrays
+        size_t rc_desc, rc_wch, rc_count, rc_amp, rc_spec, rc_part, rc_minmax, rc_oob, rc_order, rc_band_start,
+            rc_tile_next;
+        size_t slot_bytes;
+        int windows;
+    };
+    // lay[0]: nslots slots of max_batch windows; lay[1]: 2 nslots lanes of
+    // max_batch / 2 windows in the same memory (windows 0: none)
+    Layout lay[2] = {};
     // host-entry buffers
     void *d_img[2] = {nullptr, nullptr};
     size_t img_bytes[2] = {0, 0};
@@ -63,6 +73,9 @@ namespace xcg {
 // The context's plan with its tables and scratch filled in; the caller sets
 // the pair fields, the window arrays and launches with ctx_launch.
 Plan ctx_plan(const xcg_ctx *c);
+// P with its scratch pointers in lane `lane` of layout `mode` (0: slots of
+// max_batch windows, 1: half slots).
+Plan in_lane(const xcg_ctx *c, Plan P, int mode, int lane);
 // Launches the row stage of one batch (plan Q) on stream ss in place of the
 // single row launch; the host entry copies image bands between sub-launches.
 using RowsHook = std::function<xcg_status(const Plan &Q, cudaStream_t ss)>;

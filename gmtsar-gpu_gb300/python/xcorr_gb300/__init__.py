@@ -28,7 +28,7 @@ EXPORTS = ("xcg_status_string", "xcg_last_error", "xcg_default_params", "xcg_cre
            "xcg_refiner_destroy", "xcg_refiner_set_params", "xcg_refiner_get_params", "xcg_refiner_forward",
            "xcg_refiner_gradient", "xcg_refiner_train_step", "xcg_correlate_device_refined",
            "xcg_fit_offsets", "xcg_tc_gemm_check", "xcg_set_dft_form", "xcg_debug_inject_stage_timeout",
-           "xcg_fp32_fma_rate", "xcg_set_row_sharing", "xcg_set_launch_shapes")
+           "xcg_fp32_fma_rate", "xcg_set_row_sharing", "xcg_set_launch_shapes", "xcg_set_batches")
 REFINER_NPARAM = 37507
 FLAG_REFINED = 4
 FLAG_STAGE_TIMEOUT = 8
@@ -171,6 +171,8 @@ def load(path: str | None = None):
     L.xcg_set_row_sharing.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_set_launch_shapes.restype = ctypes.c_int
     L.xcg_set_launch_shapes.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]
+    L.xcg_set_batches.restype = ctypes.c_int
+    L.xcg_set_batches.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     L.xcg_fp32_fma_rate.restype = ctypes.c_int
     L.xcg_fp32_fma_rate.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
     L.xcg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int32]
@@ -241,6 +243,10 @@ class Context:
     def set_launch_shapes(self, cols_cfg: int, peak_cfg: int = 0):
         """Column- and peak-stage launch shapes (xcg_set_launch_shapes); the results do not depend on them."""
         _check(self._L.xcg_set_launch_shapes(self._h, int(cols_cfg), int(peak_cfg)))
+
+    def set_batches(self, batches: int):
+        """Batches per call, 0 automatic (xcg_set_batches); the results do not depend on it."""
+        _check(self._L.xcg_set_batches(self._h, int(batches)))
 
     def inject_stage_timeout(self):
         """The next precision-form call behaves as if a tensor-core wait had run out (error-path tests)."""

@@ -248,6 +248,14 @@ xcg_status xcg_set_row_sharing(xcg_ctx *ctx, int32_t enable);
  * 0).  Every shape gives the same bits. */
 xcg_status xcg_set_launch_shapes(xcg_ctx *ctx, int32_t cols_cfg, int32_t peak_cfg);
 
+/* Split each later call's windows into this many batches (whole strips; at
+ * most the context's max_batch windows each); 0 (default) lets the library
+ * choose.  Batches alternate between two scratch slots on their own streams,
+ * so one batch's column and peak stages overlap the next one's row stage;
+ * more batches than slots, each fitting in half a slot, run four at a time.
+ * Every split gives the same bits. */
+xcg_status xcg_set_batches(xcg_ctx *ctx, int32_t batches);
+
 /* Make later xcg_correlate_device calls on this context also write, per
  * window, the 9x9 neighbourhood of the integer peak normalised by the surface
  * maximum (DEVICE [nlocs][81]; NULL stops it): the subpixel refiner's input. */

@@ -140,3 +140,22 @@ def test_timeline_marks(pairs):
     for b in range(st.batches):
         stages = [tl[1000 + 10 * b + k] for k in range(4)]
         assert stages == sorted(stages) and stages[-1] <= tl[2]
+
+
+def test_batch_splits_same_bits(pairs):
+    """Any number of batches per call (xcg_set_batches), alternating between
+    the two scratch slots or four at a time in the half-slot lanes, gives the
+    same bits on both entries; the host entry's automatic choice for a job of
+    this size is four batches."""
+    (m1, s1), _ = pairs
+    locs = xg.grid(1024, 3072, 16, 60, 64, 64)                    # 960 windows, strips of 16
+    with xg.Context(xg.params(64, 64)) as ctx:
+        base = ctx.correlate(m1, s1, locs, strip_len=16)
+        assert ctx.stats().batches == 4
+        _same(_device(ctx, m1, s1, locs, 16), base)
+        for nb, expect in ((1, 1), (2, 2), (3, 3), (5, 5), (8, 8)):
+            ctx.set_batches(nb)
+            r = ctx.correlate(m1, s1, locs, strip_len=16)
+            assert ctx.stats().batches == expect
+            _same(r, base)
+            _same(_device(ctx, m1, s1, locs, 16), base)
