@@ -129,7 +129,19 @@ struct DftStage {
     static __device__ __forceinline__ void run(float2 *t, int i) {
         if constexpr (K < LEN / 2) {
             constexpr int M16 = K * (16 / LEN);
-            if constexpr ((M16 & 3) == 0) {       // quarter turns: exact swaps and signs
+            if constexpr (M16 == 0) {             // no rotation: a +- b on both components at once
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+                // sm_100 two-lane FP32 operations, the same rounding per
+                // component as the scalar add (a - b as b * -1 + a, rounded once)
+                const float2 a = t[i + K], b = t[i + K + LEN / 2];
+                t[i + K] = __fadd2_rn(a, b);
+                t[i + K + LEN / 2] = __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+#else
+                const float2 a = t[i + K], b = t[i + K + LEN / 2];
+                t[i + K] = make_float2(a.x + b.x, a.y + b.y);
+                t[i + K + LEN / 2] = make_float2(a.x - b.x, a.y - b.y);
+#endif
+            } else if constexpr ((M16 & 3) == 0) {   // quarter turns: exact swaps and signs
                 float2 a = t[i + K];
                 float2 b = rot16<M16, DIR>(t[i + K + LEN / 2]);
                 t[i + K] = make_float2(a.x + b.x, a.y + b.y);
