@@ -41,6 +41,23 @@ __host__ __device__ constexpr int fft_twiddle_len(int n) {
     return len;
 }
 
+// a + b and a * b + c on both components: sm_100's two-lane FP32 instructions,
+// rounded per component as the scalar ones
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __ffma2_rn(a, b, c);
+#else
+    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+#endif
+}
+
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -130,17 +147,10 @@ struct DftStage {
         if constexpr (K < LEN / 2) {
             constexpr int M16 = K * (16 / LEN);
             if constexpr (M16 == 0) {             // no rotation: a +- b on both components at once
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
-                // sm_100 two-lane FP32 operations, the same rounding per
-                // component as the scalar add (a - b as b * -1 + a, rounded once)
+                // (a - b as b * -1 + a, rounded once: the scalar difference)
                 const float2 a = t[i + K], b = t[i + K + LEN / 2];
-                t[i + K] = __fadd2_rn(a, b);
-                t[i + K + LEN / 2] = __ffma2_rn(b, make_float2(-1.f, -1.f), a);
-#else
-                const float2 a = t[i + K], b = t[i + K + LEN / 2];
-                t[i + K] = make_float2(a.x + b.x, a.y + b.y);
-                t[i + K + LEN / 2] = make_float2(a.x - b.x, a.y - b.y);
-#endif
+                t[i + K] = fadd2(a, b);
+                t[i + K + LEN / 2] = ffma2(b, make_float2(-1.f, -1.f), a);
             } else if constexpr ((M16 & 3) == 0) {   // quarter turns: exact swaps and signs
                 float2 a = t[i + K];
                 float2 b = rot16<M16, DIR>(t[i + K + LEN / 2]);
