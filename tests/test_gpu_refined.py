@@ -61,3 +61,34 @@ def test_refined_beats_the_fft_interpolation_against_truth(run):
     ey_p, ey_r = rms(yp - shift[:, 1]), rms(yr - shift[:, 1])
     assert ex_r < 0.6 * ex_p, (ex_r, ex_p)
     assert ey_r < ey_p, (ey_r, ey_p)
+
+
+def test_refined_path_any_batch_split():
+    """The refined path runs its batches through the plain path's scheduler:
+    one batch, two slots or the four half-slot lanes give the same bits."""
+    torch = pytest.importorskip("torch")
+    if not os.path.exists(WEIGHTS):
+        pytest.skip("no trained refiner weights")
+    from xcorr_gb300 import refiner_train as rt
+    dev = torch.device("cuda", 0)
+    m, s, locs, shift, snr = rt.make_tiles(32, 32, 55555, dev)
+    n = len(locs)
+    ny, nx = m.shape[0], m.shape[1]
+    dl = torch.from_numpy(locs).to(dev)
+    ref = xg.Refiner(0, max_batch=64)
+    ref.set_params(rt.load_weights(WEIGHTS))
+    st = torch.cuda.current_stream(dev).cuda_stream
+    outs = []
+    with xg.Context(xg.params(64, 64)) as ctx:
+        with pytest.raises(xg.XcgError):
+            ctx.set_batches(-1)
+        for nb in (1, 2, 3, 4, 8):
+            ctx.set_batches(nb)
+            out = torch.zeros((n, xg.RESULT_DTYPE.itemsize), dtype=torch.uint8, device=dev)
+            ctx.correlate_device_refined(ref, m.data_ptr(), nx, ny, s.data_ptr(), nx, ny, dl.data_ptr(), n,
+                                         out.data_ptr(), st, max_sigma=0.15, max_disagree=0.25)
+            torch.cuda.synchronize()
+            assert ctx.stats().batches == nb
+            outs.append(out.cpu().numpy().tobytes())
+    ref.close()
+    assert all(o == outs[0] for o in outs[1:])
