@@ -59,6 +59,21 @@ __device__ __forceinline__ float argmax_value(unsigned long long k) {
     return ord <= 1u ? 0.f : __uint_as_float(ord - 1u);
 }
 
+// best = max(best, argmax_key(v, e)), the key built only where it can win.
+// Keys order by their value word first, and every positive value's word
+// (its bits + 1) is above the words of zero, negative and NaN values (0 or 1),
+// so once best holds a positive value, a value below it cannot win; bestv is
+// that value, or -inf while best holds none (then every key is built).
+__device__ __forceinline__ void argmax_update(unsigned long long &best, float &bestv, float v, unsigned e) {
+    if (!(v < bestv)) {
+        const unsigned long long k = argmax_key(v, e);
+        if (k > best) {
+            best = k;
+            bestv = ((unsigned)(k >> 32) >= 2u) ? argmax_value(k) : -INFINITY;
+        }
+    }
+}
+
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -815,6 +830,7 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
     // and walks the output rows Y, four at a time; a warp shares Y, so each
     // KY read is one broadcast that feeds both columns
     unsigned long long best = 0ull;
+    float bestv = -INFINITY;
     const int half = nx2 / 2;
     const int tpr = half < (int)blockDim.x ? half : (int)blockDim.x;   // threads per output row
     const int rp = (int)blockDim.x / tpr;                               // rows in flight per pass
@@ -847,8 +863,7 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
                 if (yy >= ny2) break;
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
-                    const unsigned long long kk = argmax_key(re[h][j], (unsigned)(yy * nx2 + X + h * half));
-                    best = kk > best ? kk : best;
+                    argmax_update(best, bestv, re[h][j], (unsigned)(yy * nx2 + X + h * half));
                 }
             }
         }
