@@ -276,8 +276,8 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_s
     constexpr int TWL = fft_twiddle_len(N);
     constexpr int PER = N / T;
     constexpr int NH = N / 2;
-    constexpr bool HSHIFT = (LG == 1) && (N <= 256);
-    constexpr int TWS = (N <= 256) ? 2 * TWL : TWL;
+    constexpr bool HSHIFT = (LG == 1) && (N <= 512);
+    constexpr int TWS = (N <= 512) ? 2 * TWL : TWL;
     constexpr int RBP = 32;
     constexpr int GOFF = 32 / TPW;
 
@@ -916,7 +916,7 @@ static size_t segrows_smem() {
     constexpr int T = fft_lanes(N);
     constexpr int ACC = (N >= 1024) ? 1024 : 512;
     const int teams = 128 / T;
-    return fft_twiddle_len(N) * (N <= 256 ? 2 : 1) * sizeof(float2) +
+    return fft_twiddle_len(N) * (N <= 512 ? 2 : 1) * sizeof(float2) +
            (size_t)teams * (fft_padded_len(N) * sizeof(float2) + (2 * N + 32) * sizeof(float)) +
            (size_t)(128 / 32) * (ACC + 32) * sizeof(float);
 }

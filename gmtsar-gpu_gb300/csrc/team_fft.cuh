@@ -282,14 +282,19 @@ __host__ __device__ constexpr float cos32(int k) {
 }
 __host__ __device__ constexpr float sin32(int k) { return cos32(k - 8); }
 
-// HS (half-sample shift, inverse transforms of N <= 256 only): the input
-// element f = lane + T*m is first multiplied by phi(f) = exp(i pi f'/N) / N
-// (f' = f, or f - N for f >= N/2), which turns the inverse FFT into the
+// HS (half-sample shift, inverse transforms of N = 128, 256 or 512): the
+// input element f = lane + T*m is first multiplied by phi(f) = exp(i pi f'/N)
+// / N (f' = f, or f - N for f >= N/2), which turns the inverse FFT into the
 // half-sample shifted interpolation.  phi(f) = A(lane) * C(m): C(m) =
 // exp(2 pi i m / 32) / N, negated for m >= 8, is a constant multiplied here;
-// A(lane) = exp(i pi lane / N) rides on the next pass's twiddles (the pass-0
-// outputs of lane l are the next pass's inputs r = l), whose table must then
-// hold exp(-2 pi i r (k + 1/2) / N) (half_shift_twiddles).
+// A(lane) = exp(i pi lane / N) rides on the later passes' twiddles.  For
+// N <= 256 the pass-0 outputs of lane l are the next pass's inputs r = l, so
+// that pass's table holds exp(-2 pi i r (k + 1/2) / N).  For N = 512 (T = 32,
+// passes 16, 16, 2) pass 1's input r of lane j came from lane (j >> 4) + 2r:
+// the factor exp(2 pi i r / 512) goes into pass 1's table, exp(-2 pi i r
+// (k + 1/2) / 256), and the lane's common factor exp(i pi (j >> 4) / 512)
+// reaches pass 2 as its input r = j >> 4, so pass 2's table holds
+// exp(-2 pi i (k + 1/2) / 512) (put_row_phase builds these tables).
 // ZMID: the sequence is zero outside registers [N/T/4, 3N/T/4), i.e. outside
 // elements [N/4, 3N/4) (a masked column); the first pass then skips the
 // butterflies with a zero input (its 16-point DFTs see elements [4, 12) only).
@@ -301,7 +306,8 @@ __device__ __forceinline__ void team_fft_reg_pass(float2 *v, float2 *ex, const f
     constexpr int NR = N / R;
     constexpr int IT = NR / T;                 // butterflies per lane in this pass
     static_assert(IT * R * T == N, "team layout");
-    static_assert(!HS || (DIR > 0 && N / T == 16 && IT == 1 && NP == 2), "half-sample shift: N = 128 or 256");
+    static_assert(!HS || (DIR > 0 && N / T == 16 && IT == 1 && (NP == 2 || N == 512)),
+                  "half-sample shift: N = 128, 256 or 512");
     static_assert(!ZMID || (fft_radix(N, 0) == 16 && !HS), "zero outside the middle half: radix-16 first pass");
     if constexpr (PASS == 0) {
         // inputs from registers: element (lane + T*it) + NR*r = lane + T*(it + r*IT)
@@ -379,7 +385,7 @@ __device__ __forceinline__ void team_fft_reg_mid(float2 *v, float2 *ex, const fl
 }
 
 // Inverse FFT of X[f] * exp(i pi f' / N) / N (the odd samples of a 2x
-// zero-pad interpolation) for N = 128 or 256; twh: half_shift_twiddles(N).
+// zero-pad interpolation) for N = 128, 256 or 512; twh: the tables put_row_phase builds.
 template <int N>
 __device__ __forceinline__ void team_ifft_half_shift(float2 *v, float2 *ex, const float2 *twh, int lane) {
     team_fft_reg_pass<N, +1, 0, true>(v, ex, twh, 1, lane);

@@ -132,8 +132,8 @@ __global__ void __launch_bounds__(128, (N >= 1024) ? 2 : (N >= 512 ? 3 : 4)) k_r
 
     // ri = 2 rows of up to 256 points: the phase of the interpolation rides
     // on a second twiddle table (team_ifft_half_shift)
-    constexpr bool HSHIFT = (LG == 1) && (N <= 256);
-    constexpr int TWS = (N <= 256) ? 2 * TWL : TWL;     // twiddle entries in shared memory
+    constexpr bool HSHIFT = (LG == 1) && (N <= 512);
+    constexpr int TWS = (N <= 512) ? 2 * TWL : TWL;     // twiddle entries in shared memory
 
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
@@ -895,14 +895,20 @@ __global__ void __launch_bounds__(256) k_subpix(Plan P) {
 
 int put_row_phase(float2 *dst, int n, int ri) {
     if (ri == 1) { dst[0] = make_float2(0.f, 0.f); return 1; }
-    if (ri == 2 && n <= 256) {
-        // [(r-1)*16 + k] = exp(-2 pi i r (k + 1/2) / n): the second pass's
-        // twiddle with the lane factor exp(i pi r / n) folded in
-        const int r1 = n / 16;                       // radix of the second pass
+    if (ri == 2 && n <= 512) {
+        // [(r-1)*16 + k] = exp(-2 pi i r (k + 1/2) / (16 r1)): the second
+        // pass's twiddle with the lane factor of the half-sample shift folded
+        // in; for n = 512 the third pass's [240 + k] = exp(-2 pi i (k + 1/2) / 512)
+        const int r1 = n <= 256 ? n / 16 : 16;       // radix of the second pass
         int o = 0;
         for (int r = 1; r < r1; r++)
             for (int k = 0; k < 16; k++) {
-                const double a = -2.0 * M_PI * r * (k + 0.5) / n;
+                const double a = -2.0 * M_PI * r * (k + 0.5) / (16.0 * r1);
+                dst[o++] = make_float2((float)cos(a), (float)sin(a));
+            }
+        if (n == 512)
+            for (int k = 0; k < 256; k++) {
+                const double a = -2.0 * M_PI * (k + 0.5) / 512.0;
                 dst[o++] = make_float2((float)cos(a), (float)sin(a));
             }
         for (; o < n; o++) dst[o] = make_float2(0.f, 0.f);
@@ -923,7 +929,7 @@ static size_t rows_smem() {
     constexpr int T = fft_lanes(N);
     constexpr int ACC = (N >= 1024) ? 1024 : 512;
     const int teams = 128 / T;
-    return fft_twiddle_len(N) * (N <= 256 ? 2 : 1) * sizeof(float2) +
+    return fft_twiddle_len(N) * (N <= 512 ? 2 : 1) * sizeof(float2) +
            (size_t)teams * (fft_padded_len(N) * sizeof(float2) + (2 * N + 32) * sizeof(float)) +
            (size_t)(128 / 32) * 2 * (ACC + 32) * sizeof(float);
 }

@@ -64,7 +64,7 @@ struct TableSet {
 };
 
 // Entries put_row_phase writes for n-point rows and factor ri.
-int row_phase_len(int n, int ri) { return ri == 1 ? 1 : (ri == 2 && n <= 256) ? n : (ri - 1) * n; }
+int row_phase_len(int n, int ri) { return ri == 1 ? 1 : (ri == 2 && n <= 512) ? n : (ri - 1) * n; }
 
 TableSet table_set(int npx, int npy, int ri, int xs, int ys, int n2x, int nx2, int n2y, int ny2) {
     TableSet t;
@@ -114,10 +114,16 @@ __device__ float2 stockham_twiddle(int n, int i) {
 // Entry i of the row kernel's range-interpolation table (put_row_phase).
 __device__ float2 row_phase(int n, int ri, int i) {
     if (ri == 1) return make_float2(0.f, 0.f);
-    if (ri == 2 && n <= 256) {
+    if (ri == 2 && n <= 512) {
+        const int r1 = n <= 256 ? n / 16 : 16;     // radix of the second pass
         const int r = i / 16 + 1, k = i % 16;
-        if (r >= n / 16) return make_float2(0.f, 0.f);
-        const double a = -2.0 * M_PI * r * (k + 0.5) / n;
+        if (r < r1) {
+            const double a = -2.0 * M_PI * r * (k + 0.5) / (16.0 * r1);
+            return make_float2((float)cos(a), (float)sin(a));
+        }
+        const int k3 = i - 16 * (r1 - 1);           // n = 512: the third pass's entries
+        if (n != 512 || k3 >= 256) return make_float2(0.f, 0.f);
+        const double a = -2.0 * M_PI * (k3 + 0.5) / 512.0;
         return make_float2((float)cos(a), (float)sin(a));
     }
     const int q = i / n + 1, f = i % n;
