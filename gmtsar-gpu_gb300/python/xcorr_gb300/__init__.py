@@ -268,7 +268,7 @@ class Context:
             if self.params.format == 1 and (a.dtype != np.float32 or a.ndim != 2):
                 raise ValueError(f"{name}: -real images are (ny, nx) float32 arrays, got {a.dtype} {a.shape}")
         locs = np.ascontiguousarray(locs, dtype=np.int32).reshape(-1, 2)
-        out = np.zeros(len(locs), dtype=RESULT_DTYPE)
+        out = np.empty(len(locs), dtype=RESULT_DTYPE)        # the call writes every record
         _check(self._L.xcg_correlate(self._h, master.ctypes.data, master.shape[1], master.shape[0],
                                      slave.ctypes.data, slave.shape[1], slave.shape[0],
                                      int(x_offset), int(y_offset), float(astretcha),
