@@ -677,23 +677,54 @@ __global__ void __launch_bounds__(NT, MINB) k_peak(Plan P) {
     }
     long long sn = 0, s1 = 0, s2 = 0;
     constexpr int NXC = N / 2;          // nx_corr = 2 xsearch = npx / 2
-    constexpr int GU = 8;               // loads in flight per thread and operand
-    const int ntot = P.ny_corr * NXC;   // a multiple of NT * GU for windows of 64 and more
-    for (int i0 = threadIdx.x; i0 < ntot; i0 += NT * GU) {
-        float va[GU], vb[GU];
-#pragma unroll
-        for (int u = 0; u < GU; u++) {
-            const int i = i0 + u * NT;
-            const int r = i / NXC, cc = i - r * NXC;
-            // 32 x 32 windows (1024 samples) fill only half of one NT x GU pass
-            const bool in = (NXC >= 64) || (i < ntot);
-            va[u] = in ? __ldg(a1 + (size_t)r * N + cc) : m1f;
-            vb[u] = in ? __ldg(a2 + (size_t)r * a2s + cc) : m2f;
+    if constexpr (N <= 256) {
+        // The rows are staged by cp.async in the transforms' exchange buffers,
+        // free from here on: RRM rows of both operands per round, all of them
+        // in flight at once without holding registers (the peak stage of
+        // these sizes is latency-bound: 0.107 -> 0.098 ms per 1000 windows of
+        // 128 x 128; the 512-point stage, at several waves, is faster with the
+        // register loads below).  The sums are integers, so their order does
+        // not change them.
+        constexpr int FBF = (NT / T) * PADN * 2;        // floats of the exchange buffers
+        constexpr int RRM = FBF / (2 * NXC);            // rows of both operands per round
+        static_assert(RRM >= 1 && NXC % 4 == 0, "staging rows");
+        float *sa = reinterpret_cast<float *>(fb), *sb = sa + RRM * NXC;
+        for (int r0 = 0; r0 < P.ny_corr; r0 += RRM) {
+            const int n = min(RRM, P.ny_corr - r0) * NXC;
+            for (int i = threadIdx.x; i < n; i += NT) {      // master rows at the peak offset: any alignment
+                const int r = i / NXC, cc = i - r * NXC;
+                cp_async4(sa + i, a1 + (size_t)(r0 + r) * N + cc);
+            }
+            for (int i = threadIdx.x; i < n / 4; i += NT) {  // the slave's centre: 16-byte aligned rows
+                const int e = 4 * i, r = e / NXC, cc = e - r * NXC;
+                cp_async16(sb + e, a2 + (size_t)(r0 + r) * a2s + cc);
+            }
+            cp_async_commit();
+            cp_async_wait<0>();
+            __syncthreads();
+            for (int i = threadIdx.x; i < n; i += NT) {
+                const long long ia = (long long)(int)(sa[i] - m1f), ib = (long long)(int)(sb[i] - m2f);
+                sn += ia * ib; s1 += ia * ia; s2 += ib * ib;
+            }
+            __syncthreads();             // read before the next round's copies land
         }
+    } else {
+        constexpr int GU = 8;            // loads in flight per thread and operand
+        const int ntot = P.ny_corr * NXC;   // a multiple of NT * GU
+        for (int i0 = threadIdx.x; i0 < ntot; i0 += NT * GU) {
+            float va[GU], vb[GU];
 #pragma unroll
-        for (int u = 0; u < GU; u++) {
-            const long long ia = (long long)(int)(va[u] - m1f), ib = (long long)(int)(vb[u] - m2f);
-            sn += ia * ib; s1 += ia * ia; s2 += ib * ib;
+            for (int u = 0; u < GU; u++) {
+                const int i = i0 + u * NT;
+                const int r = i / NXC, cc = i - r * NXC;
+                va[u] = __ldg(a1 + (size_t)r * N + cc);
+                vb[u] = __ldg(a2 + (size_t)r * a2s + cc);
+            }
+#pragma unroll
+            for (int u = 0; u < GU; u++) {
+                const long long ia = (long long)(int)(va[u] - m1f), ib = (long long)(int)(vb[u] - m2f);
+                sn += ia * ib; s1 += ia * ia; s2 += ib * ib;
+            }
         }
     }
     sn = warp_sum_i64(sn); s1 = warp_sum_i64(s1); s2 = warp_sum_i64(s2);
